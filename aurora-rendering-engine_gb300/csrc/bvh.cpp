@@ -1,0 +1,263 @@
+// bvh.cpp — binned SAH build (host), then a layout pass that places the top
+// levels breadth-first (so the first nodes can be staged in shared memory)
+// and every deeper subtree depth-first, with each sibling pair on one
+// 64-byte line.
+#include "bvh.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <numeric>
+
+#include "core.h"
+
+namespace are_core {
+namespace {
+
+struct TmpNode {
+	double lo[3], hi[3];
+	int32_t left = -1, right = -1;  // children in tmp, -1 for leaves
+	int32_t first = 0, count = 0;   // range in `idx`
+	int32_t depth = 0;
+};
+
+constexpr int NBINS = 16;
+
+inline double area(const double lo[3], const double hi[3]) {
+	double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+	if (dx < 0 || dy < 0 || dz < 0) return 0.0;
+	return 2.0 * (dx * dy + dy * dz + dz * dx);
+}
+
+struct Builder {
+	const std::vector<PrimBox> &boxes;
+	std::vector<double> cen;  // 3 per prim
+	std::vector<int32_t> idx;
+	std::vector<TmpNode> nodes;
+	int leaf_size;
+	int max_depth = 0;
+
+	Builder(const std::vector<PrimBox> &b, int leaf) : boxes(b), leaf_size(leaf) {}
+
+	void bounds(int32_t first, int32_t count, double lo[3], double hi[3], double clo[3], double chi[3]) const {
+		for (int k = 0; k < 3; ++k) {
+			lo[k] = clo[k] = std::numeric_limits<double>::infinity();
+			hi[k] = chi[k] = -std::numeric_limits<double>::infinity();
+		}
+		for (int32_t i = first; i < first + count; ++i) {
+			const PrimBox &b = boxes[idx[i]];
+			for (int k = 0; k < 3; ++k) {
+				lo[k] = std::min(lo[k], b.lo[k]);
+				hi[k] = std::max(hi[k], b.hi[k]);
+				double c = cen[3 * idx[i] + k];
+				clo[k] = std::min(clo[k], c);
+				chi[k] = std::max(chi[k], c);
+			}
+		}
+	}
+
+	// returns the split position (index in [first, first+count)) or -1 for a leaf
+	int32_t split(int32_t first, int32_t count, int depth, const double lo[3], const double hi[3],
+		const double clo[3], const double chi[3]) {
+		if (count <= 1) return -1;
+		int axis = 0;
+		for (int k = 1; k < 3; ++k)
+			if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+		double ext = chi[axis] - clo[axis];
+		auto median = [&]() {
+			int32_t mid = first + count / 2;
+			std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count,
+				[&](int32_t a, int32_t b) {
+					double ca = cen[3 * a + axis], cb = cen[3 * b + axis];
+					return ca < cb || (ca == cb && a < b);
+				});
+			return mid;
+		};
+		if (depth >= MAX_BVH_DEPTH - 2) return count <= leaf_size ? -1 : median();
+		if (!(ext > 0)) return count <= leaf_size ? -1 : median();
+		// binned SAH along the widest centroid axis
+		struct Bin {
+			double lo[3], hi[3];
+			int32_t n;
+		} bins[NBINS];
+		for (auto &b : bins) {
+			for (int k = 0; k < 3; ++k) b.lo[k] = std::numeric_limits<double>::infinity(), b.hi[k] = -b.lo[k];
+			b.n = 0;
+		}
+		double scale = NBINS / ext;
+		auto bin_of = [&](int32_t p) {
+			int b = (int)((cen[3 * p + axis] - clo[axis]) * scale);
+			return std::min(std::max(b, 0), NBINS - 1);
+		};
+		for (int32_t i = first; i < first + count; ++i) {
+			Bin &b = bins[bin_of(idx[i])];
+			const PrimBox &pb = boxes[idx[i]];
+			for (int k = 0; k < 3; ++k) b.lo[k] = std::min(b.lo[k], pb.lo[k]), b.hi[k] = std::max(b.hi[k], pb.hi[k]);
+			++b.n;
+		}
+		double right_area[NBINS];
+		int32_t right_n[NBINS];
+		double rlo[3], rhi[3];
+		for (int k = 0; k < 3; ++k) rlo[k] = std::numeric_limits<double>::infinity(), rhi[k] = -rlo[k];
+		int32_t rn = 0;
+		for (int b = NBINS - 1; b > 0; --b) {
+			for (int k = 0; k < 3; ++k) rlo[k] = std::min(rlo[k], bins[b].lo[k]), rhi[k] = std::max(rhi[k], bins[b].hi[k]);
+			rn += bins[b].n;
+			right_area[b] = area(rlo, rhi);
+			right_n[b] = rn;
+		}
+		double llo[3], lhi[3];
+		for (int k = 0; k < 3; ++k) llo[k] = std::numeric_limits<double>::infinity(), lhi[k] = -llo[k];
+		int32_t ln = 0;
+		double best = std::numeric_limits<double>::infinity();
+		int best_b = -1;
+		for (int b = 1; b < NBINS; ++b) {
+			for (int k = 0; k < 3; ++k)
+				llo[k] = std::min(llo[k], bins[b - 1].lo[k]), lhi[k] = std::max(lhi[k], bins[b - 1].hi[k]);
+			ln += bins[b - 1].n;
+			if (ln == 0 || right_n[b] == 0) continue;
+			double c = area(llo, lhi) * ln + right_area[b] * right_n[b];
+			if (c < best) best = c, best_b = b;
+		}
+		double parent = area(lo, hi);
+		double leaf_cost = (double)count;
+		double split_cost = parent > 0 ? 0.5 + best / parent : std::numeric_limits<double>::infinity();
+		if (best_b < 0) return count <= leaf_size ? -1 : median();
+		if (count <= leaf_size && split_cost >= leaf_cost) return -1;
+		auto it = std::partition(idx.begin() + first, idx.begin() + first + count,
+			[&](int32_t p) { return bin_of(p) < best_b; });
+		int32_t mid = (int32_t)(it - idx.begin());
+		if (mid == first || mid == first + count) return median();
+		return mid;
+	}
+
+	void build() {
+		int32_t n = (int32_t)boxes.size();
+		cen.resize(3 * (size_t)n);
+		idx.resize(n);
+		std::iota(idx.begin(), idx.end(), 0);
+		for (int32_t i = 0; i < n; ++i)
+			for (int k = 0; k < 3; ++k) cen[3 * i + k] = 0.5 * (boxes[i].lo[k] + boxes[i].hi[k]);
+		nodes.reserve(2 * (size_t)n);
+		struct Job {
+			int32_t node, first, count, depth;
+		};
+		std::vector<Job> stack;
+		nodes.push_back(TmpNode{});
+		stack.push_back({ 0, 0, n, 0 });
+		while (!stack.empty()) {
+			Job j = stack.back();
+			stack.pop_back();
+			double lo[3], hi[3], clo[3], chi[3];
+			bounds(j.first, j.count, lo, hi, clo, chi);
+			TmpNode &t = nodes[j.node];
+			std::memcpy(t.lo, lo, sizeof lo);
+			std::memcpy(t.hi, hi, sizeof hi);
+			t.depth = j.depth;
+			max_depth = std::max(max_depth, j.depth);
+			int32_t mid = split(j.first, j.count, j.depth, lo, hi, clo, chi);
+			if (mid < 0) {
+				nodes[j.node].first = j.first;
+				nodes[j.node].count = j.count;
+				continue;
+			}
+			int32_t l = (int32_t)nodes.size();
+			nodes.push_back(TmpNode{});
+			nodes.push_back(TmpNode{});
+			nodes[j.node].left = l;
+			nodes[j.node].right = l + 1;
+			stack.push_back({ l + 1, mid, j.first + j.count - mid, j.depth + 1 });
+			stack.push_back({ l, j.first, mid - j.first, j.depth + 1 });
+		}
+	}
+};
+
+}  // namespace
+
+BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
+	BvhResult r;
+	if (leaf_size <= 0) leaf_size = 4;
+	if (leaf_size > 64) leaf_size = 64;
+	if (boxes.empty()) {
+		r.n_nodes = 2;
+		r.nodes.assign(16, 0.0f);
+		// an empty leaf whose box is inverted: nothing is ever hit
+		for (int k = 0; k < 3; ++k) r.nodes[k] = 1.0f, r.nodes[4 + k] = -1.0f;
+		return r;
+	}
+	Builder b(boxes, leaf_size);
+	b.build();
+
+	double scale = 0.0;
+	for (const PrimBox &pb : boxes)
+		for (int k = 0; k < 3; ++k) scale = std::max(scale, std::max(std::fabs(pb.lo[k]), std::fabs(pb.hi[k])));
+	r.box_pad = (float)(scale * std::ldexp(1.0, -19)) + 1e-30f;
+
+	// layout: root at 0, padding at 1, sibling pairs at even indices; pairs are
+	// allocated breadth-first until 1024 nodes exist, depth-first afterwards.
+	const size_t ntmp = b.nodes.size();
+	std::vector<int32_t> slot(ntmp, -1);
+	slot[0] = 0;
+	int32_t next = 2;
+	std::deque<int32_t> work;
+	work.push_back(0);
+	while (!work.empty()) {
+		int32_t t;
+		if (next < SMEM_NODES) {
+			t = work.front();
+			work.pop_front();
+		} else {
+			t = work.back();
+			work.pop_back();
+		}
+		const TmpNode &tn = b.nodes[t];
+		if (tn.left < 0) continue;
+		slot[tn.left] = next;
+		slot[tn.right] = next + 1;
+		next += 2;
+		if (next < SMEM_NODES) {
+			work.push_back(tn.left);
+			work.push_back(tn.right);
+		} else {  // depth-first: visit the left child next
+			work.push_back(tn.right);
+			work.push_back(tn.left);
+		}
+	}
+	r.n_nodes = next;
+	r.nodes.assign(8 * (size_t)next, 0.0f);
+	// padding node 1: inverted box, never hit
+	for (int k = 0; k < 3; ++k) r.nodes[8 + k] = 1.0f, r.nodes[12 + k] = -1.0f;
+
+	// leaves keep the primitive ranges of the build order
+	r.order = b.idx;
+	int32_t max_leaf = 0;
+	for (size_t t = 0; t < ntmp; ++t) {
+		const TmpNode &tn = b.nodes[t];
+		float *o = &r.nodes[8 * (size_t)slot[t]];
+		for (int k = 0; k < 3; ++k) {
+			float lo = (float)tn.lo[k], hi = (float)tn.hi[k];
+			if ((double)lo > tn.lo[k]) lo = std::nextafter(lo, -INFINITY);
+			if ((double)hi < tn.hi[k]) hi = std::nextafter(hi, INFINITY);
+			o[k] = lo - r.box_pad;
+			o[4 + k] = hi + r.box_pad;
+		}
+		int32_t a, bb;
+		if (tn.left < 0) {
+			a = tn.first;
+			bb = tn.count;
+			max_leaf = std::max(max_leaf, tn.count);
+		} else {
+			a = slot[tn.left];
+			bb = 0;
+		}
+		std::memcpy(&o[3], &a, 4);
+		std::memcpy(&o[7], &bb, 4);
+	}
+	r.depth = b.max_depth;
+	r.max_leaf = max_leaf;
+	return r;
+}
+
+}  // namespace are_core

@@ -1,0 +1,609 @@
+// render.cu — the wavefront path tracer and the batched closest-hit query.
+//
+// Replaces rt.cpp render() / trace() / intersect() (experiments/rt.cpp:209-374).
+// The reference walks pixels one by one and recurses per path on one host
+// thread.  Here a pool of P paths lives in HBM as SoA records and every
+// wavefront iteration runs three kernels over compacted queues:
+//
+//   intersect : closest hit of every queued ray (BVH, top levels in smem)
+//   shade     : emission + material scatter + Russian roulette; surviving
+//               paths append their next ray to the output queue, finished
+//               paths append their slot to the terminated list (warp-ballot
+//               compaction, one atomic per warp)
+//   generate  : finished paths add their radiance to the slot's Kahan sum,
+//               take their next sample (or next work item) and append a new
+//               camera ray to the output queue
+//
+// Work items are (pixel, chunk of samples); each item's samples run in one
+// slot in order, so the per-item Kahan sums - and the image - do not depend
+// on scheduling.  `resolve` adds the items of each pixel in chunk order.
+// Iterations are captured K at a time in a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "scene.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace are_core {
+
+constexpr int GRAPH_ITERS = 16;  // iterations per graph launch (even)
+constexpr int BLOCK = 256;
+
+struct Wave {
+	// queues: ray records are (o.xyz, slot bits) and (d.xyz, 0)
+	float4 *qo[2], *qd[2];
+	float4 *hit;      // (t, leaf bits, u, v)
+	float4 *st0;      // (beta.xyz, depth | j << 8)
+	float4 *st1;      // (L.xyz, item bits)
+	float4 *acc_s;    // Kahan sum (xyz) per slot
+	float4 *acc_c;    // Kahan compensation per slot
+	float4 *acc_q;    // sum of squares per slot
+	int32_t *term;    // terminated slots
+	unsigned *cnt;    // [0],[1] queue sizes, [2] terminated, [3] next work item, [4] error word
+	unsigned long long *stat;  // [0] segments, [1] samples
+	float4 *item_s;   // per work item: sum (xyz)
+	float4 *item_q;   // per work item: sum of squares
+	int32_t P;
+	int32_t npix, spp, chunk, nchunk;
+	int64_t n_items;
+	int32_t max_depth, rr_depth;
+	float t_min;
+	uint64_t seed;
+	CameraFrame cam;
+};
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append: every lane of the (converged) warp calls this.
+__device__ __forceinline__ unsigned warp_append(unsigned *counter, bool pred) {
+	unsigned m = __ballot_sync(0xffffffffu, pred);
+	unsigned base = 0;
+	if (m) {
+		if (lane_id() == (unsigned)(__ffs(m) - 1)) base = atomicAdd(counter, (unsigned)__popc(m));
+		base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+	}
+	return base + (unsigned)__popc(m & ((1u << lane_id()) - 1u));
+}
+
+__device__ __forceinline__ void stage_nodes(const DevScene &S, float4 *snodes, int &n_snodes) {
+	n_snodes = min(S.n_nodes, SMEM_NODES);
+	for (int i = threadIdx.x; i < 2 * n_snodes; i += blockDim.x) snodes[i] = __ldg(S.nodes + i);
+	__syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// batched closest hit (are_intersect)
+
+__global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const float4 *__restrict__ rays, int64_t n,
+	float4 *__restrict__ hits, unsigned *err_word) {
+	__shared__ float4 snodes[2 * SMEM_NODES];
+	int n_snodes;
+	stage_nodes(S, snodes, n_snodes);
+	uint32_t err = 0;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+		Hit h;
+		if (S.n_prims > 0) {
+			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
+		} else {
+			h.leaf = -1;
+		}
+		hits[i] = h.leaf >= 0 ? make_float4(h.t, __int_as_float(h.gid), h.u, h.v)
+							  : make_float4(__int_as_float(0x7f800000), __int_as_float(-1), 0.f, 0.f);
+	}
+	if (err) atomicOr(err_word, err);
+}
+
+// ---------------------------------------------------------------------------
+// wavefront kernels
+
+__device__ __forceinline__ void start_sample(const Wave &W, int slot, int64_t item, int j) {
+	// j-th sample of work item `item` begins in `slot`: state only
+	W.st0[slot] = make_float4(1.f, 1.f, 1.f, __int_as_float(j << 8));
+	W.st1[slot] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)item));
+}
+
+__device__ __forceinline__ void item_coords(const Wave &W, int64_t item, int j, int &pixel, int &sample) {
+	pixel = (int)(item % W.npix);
+	sample = (int)(item / W.npix) * W.chunk + j;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
+	// slot s takes work item s; its first camera ray goes to queue 0 position s
+	for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < W.P; s += gridDim.x * blockDim.x) {
+		W.acc_s[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+		W.acc_c[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+		W.acc_q[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+		if (s >= n_first) continue;
+		start_sample(W, s, s, 0);
+		int pixel, sample;
+		item_coords(W, s, 0, pixel, sample);
+		uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+		f3 o, d;
+		camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
+		W.qo[0][s] = make_float4(o.x, o.y, o.z, __int_as_float(s));
+		W.qd[0][s] = make_float4(d.x, d.y, d.z, 0.f);
+	}
+}
+
+__global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par) {
+	__shared__ float4 snodes[2 * SMEM_NODES];
+	int n_snodes;
+	const unsigned n = W.cnt[par];
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		W.cnt[par ^ 1] = 0;  // output queue of this iteration
+		W.cnt[2] = 0;        // terminated list
+		atomicAdd(&W.stat[0], (unsigned long long)n);
+	}
+	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
+	stage_nodes(S, snodes, n_snodes);
+	const float4 *__restrict__ qo = W.qo[par];
+	const float4 *__restrict__ qd = W.qd[par];
+	uint32_t err = 0;
+	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		float4 r0 = qo[i], r1 = qd[i];
+		Hit h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, __int_as_float(0x7f800000), err);
+		W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+	}
+	if (err) atomicOr(&W.cnt[4], err);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
+	const unsigned n = W.cnt[par];
+	const float4 *__restrict__ qo = W.qo[par];
+	const float4 *__restrict__ qd = W.qd[par];
+	float4 *__restrict__ oo = W.qo[par ^ 1];
+	float4 *__restrict__ od = W.qd[par ^ 1];
+	uint32_t err = 0;
+	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		unsigned i = base + threadIdx.x;
+		bool valid = i < n;
+		bool cont = false, term = false;
+		int slot = 0;
+		f3 p, nd;
+		if (valid) {
+			float4 r0 = qo[i], r1 = qd[i];
+			float4 h = W.hit[i];
+			slot = __float_as_int(r0.w);
+			float4 s0 = W.st0[slot], s1 = W.st1[slot];
+			f3 beta = ld3(s0), L = ld3(s1);
+			int meta = __float_as_int(s0.w);
+			int depth = meta & 0xff, j = meta >> 8;
+			int64_t item = (int64_t)(unsigned)__float_as_int(s1.w);
+			f3 o = ld3(r0), d = ld3(r1);
+			int leaf = __float_as_int(h.y);
+			if (leaf < 0) {
+				L = add(L, mulv(beta, background(S, d)));
+			} else {
+				int pixel, sample;
+				item_coords(W, item, j, pixel, sample);
+				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+				Surface sf = surface_at(S, leaf, o, d, h.x, h.z, h.w);
+				cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd);
+				if (cont && depth + 1 >= W.max_depth) cont = false;
+				p = sf.p;
+				if (cont) {
+					W.st0[slot] = make_float4(beta.x, beta.y, beta.z, __int_as_float((depth + 1) | (j << 8)));
+				}
+			}
+			term = !cont;
+			W.st1[slot] = make_float4(L.x, L.y, L.z, s1.w);
+		}
+		unsigned pos = warp_append(&W.cnt[par ^ 1], cont);
+		if (cont) {
+			if (pos < (unsigned)W.P) {
+				oo[pos] = make_float4(p.x, p.y, p.z, __int_as_float(slot));
+				od[pos] = make_float4(nd.x, nd.y, nd.z, 0.f);
+			} else {
+				err |= ERR_QUEUE_OVERFLOW;
+			}
+		}
+		unsigned tp = warp_append(&W.cnt[2], term);
+		if (term) {
+			if (tp < (unsigned)W.P)
+				W.term[tp] = slot;
+			else
+				err |= ERR_QUEUE_OVERFLOW;
+		}
+	}
+	if (err) atomicOr(&W.cnt[4], err);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
+	const unsigned n = W.cnt[2];
+	float4 *__restrict__ oo = W.qo[par ^ 1];
+	float4 *__restrict__ od = W.qd[par ^ 1];
+	uint32_t err = 0;
+	unsigned long long done = 0;
+	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		unsigned i = base + threadIdx.x;
+		bool valid = i < n;
+		bool emit = false;
+		int slot = 0;
+		f3 o, d;
+		if (valid) {
+			slot = W.term[i];
+			float4 s0 = W.st0[slot], s1 = W.st1[slot];
+			int j = __float_as_int(s0.w) >> 8;
+			int64_t item = (int64_t)(unsigned)__float_as_int(s1.w);
+			f3 L = ld3(s1);
+			if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
+				err |= ERR_NONFINITE;
+				L = f3{ 0.f, 0.f, 0.f };
+			}
+			// Kahan accumulation of this path's radiance into the slot
+			float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
+			float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
+			float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
+			cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
+			sm = make_float4(ts[0], ts[1], ts[2], 0.f);
+			q = make_float4(q.x + L.x * L.x, q.y + L.y * L.y, q.z + L.z * L.z, 0.f);
+			++done;
+			++j;
+			int chunk_len = min(W.chunk, W.spp - (int)(item / W.npix) * W.chunk);
+			if (j >= chunk_len) {
+				// item complete: publish its sums, take the next item
+				W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
+				W.item_q[item] = q;
+				sm = cm = q = make_float4(0.f, 0.f, 0.f, 0.f);
+				item = (int64_t)atomicAdd(&W.cnt[3], 1u);
+				j = 0;
+			}
+			W.acc_s[slot] = sm;
+			W.acc_c[slot] = cm;
+			W.acc_q[slot] = q;
+			if (item < W.n_items) {
+				start_sample(W, slot, item, j);
+				int pixel, sample;
+				item_coords(W, item, j, pixel, sample);
+				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+				camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
+				emit = true;
+			}
+		}
+		unsigned pos = warp_append(&W.cnt[par ^ 1], emit);
+		if (emit) {
+			if (pos < (unsigned)W.P) {
+				oo[pos] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
+				od[pos] = make_float4(d.x, d.y, d.z, 0.f);
+			} else {
+				err |= ERR_QUEUE_OVERFLOW;
+			}
+		}
+	}
+	if (done) atomicAdd(&W.stat[1], done);
+	if (err) atomicOr(&W.cnt[4], err);
+}
+
+// mean and variance of the mean per pixel from the per-item sums, in chunk order
+__global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ var, int clamp) {
+	for (int px = blockIdx.x * blockDim.x + threadIdx.x; px < W.npix; px += gridDim.x * blockDim.x) {
+		float s[3] = { 0.f, 0.f, 0.f }, c[3] = { 0.f, 0.f, 0.f }, q[3] = { 0.f, 0.f, 0.f };
+		for (int ch = 0; ch < W.nchunk; ++ch) {
+			int64_t it = (int64_t)ch * W.npix + px;
+			float4 a = W.item_s[it], b = W.item_q[it];
+			float v[3] = { a.x, a.y, a.z }, w[3] = { b.x, b.y, b.z };
+			for (int k = 0; k < 3; ++k) {
+				float y = v[k] - c[k];
+				float t = s[k] + y;
+				c[k] = (t - s[k]) - y;
+				s[k] = t;
+				q[k] += w[k];
+			}
+		}
+		float n = (float)W.spp;
+		for (int k = 0; k < 3; ++k) {
+			float m = s[k] / n;
+			if (var) {
+				float v = W.spp > 1 ? (q[k] - n * m * m) / (n - 1.f) / n : 0.f;
+				var[3 * (size_t)px + k] = v > 0.f ? v : 0.f;
+			}
+			if (clamp) m = fminf(fmaxf(m, 0.f), 1.f);
+			rgb[3 * (size_t)px + k] = m;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+are_status bad(const std::string &m) {
+	set_error(m);
+	return ARE_ERR_INVALID_ARGUMENT;
+}
+
+int grid_for(const void *kernel, int n_sms, size_t smem = 0) {
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem);
+	return std::max(1, per_sm) * n_sms;
+}
+
+void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) {
+	// rt.cpp:339-343: forward, right = forward x up, up' = right x forward
+	float fw[3] = { c.lookat[0] - c.lookfrom[0], c.lookat[1] - c.lookfrom[1], c.lookat[2] - c.lookfrom[2] };
+	auto nrm = [](float *v) {
+		float l = 1.0f / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+		v[0] *= l, v[1] *= l, v[2] *= l;
+	};
+	nrm(fw);
+	float rt[3] = { fw[1] * c.vup[2] - fw[2] * c.vup[1], fw[2] * c.vup[0] - fw[0] * c.vup[2],
+		fw[0] * c.vup[1] - fw[1] * c.vup[0] };
+	nrm(rt);
+	float up[3] = { rt[1] * fw[2] - rt[2] * fw[1], rt[2] * fw[0] - rt[0] * fw[2], rt[0] * fw[1] - rt[1] * fw[0] };
+	for (int k = 0; k < 3; ++k) f.pos[k] = c.lookfrom[k], f.fwd[k] = fw[k], f.right[k] = rt[k], f.up[k] = up[k];
+	f.aspect = (float)w / (float)h;
+	f.scale = std::tan(c.vfov_deg * 0.5f * (float)3.14159265358979323846 / 180.f);
+	f.lens = c.aperture > 0.0f;
+	f.lens_r = c.aperture * 0.5f;
+	f.focus = c.focus_dist;
+	f.jitter = !(flags & ARE_FLAG_NO_JITTER);
+	f.width = w;
+	f.height = h;
+}
+
+template <class T>
+T *carve(char *&p, size_t count) {
+	T *r = (T *)p;
+	p += (count * sizeof(T) + 255) & ~(size_t)255;
+	return r;
+}
+
+}  // namespace
+
+are_status render(are_scene *sc, const are_camera *cam, const are_render_params *prm, float *rgb, float *var,
+	are_render_stats *stats) {
+	if (!sc || !cam || !prm || !rgb) return bad("null scene, camera, params or output");
+	const are_render_params &p = *prm;
+	if (p.width <= 0 || p.height <= 0 || p.spp <= 0 || p.max_depth <= 0 || p.max_depth > 255)
+		return bad("width, height, spp must be > 0 and max_depth in [1, 255]");
+	if ((int64_t)p.width * p.height > (1 << 26)) return bad("image too large (max 2^26 pixels)");
+	if (p.estimator != ARE_EST_PATH) return bad("estimator not supported by this entry point");
+	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");
+	if (!(p.t_min >= 0.0f) || !std::isfinite(p.t_min)) return bad("t_min must be finite and >= 0");
+	cudaSetDevice(sc->device);
+
+	Wave W{};
+	W.npix = p.width * p.height;
+	W.spp = p.spp;
+	int64_t total = (int64_t)W.npix * p.spp;
+	int P = p.pool_size > 0 ? p.pool_size : (1 << 20);
+	if (P > (1 << 24)) return bad("pool_size too large (max 2^24)");
+	int chunk = p.chunk;
+	if (chunk <= 0) chunk = (int)std::min<int64_t>(64, std::max<int64_t>(1, total / (4 * (int64_t)P)));
+	chunk = std::min(chunk, p.spp);
+	W.chunk = chunk;
+	W.nchunk = (p.spp + chunk - 1) / chunk;
+	W.n_items = (int64_t)W.npix * W.nchunk;
+	if (W.n_items >= (int64_t)UINT32_MAX - (int64_t)P) return bad("too many work items; raise chunk");
+	P = (int)std::min<int64_t>(P, W.n_items);
+	P = (P + 31) & ~31;
+	W.P = P;
+	W.max_depth = p.max_depth;
+	W.rr_depth = p.rr_depth;
+	W.t_min = p.t_min;
+	W.seed = p.seed;
+	camera_frame(*cam, p.width, p.height, p.flags, W.cam);
+
+	// workspace
+	size_t need = 0;
+	{
+		char *z = nullptr;
+		for (int q = 0; q < 2; ++q) carve<float4>(z, P), carve<float4>(z, P);
+		carve<float4>(z, P);  // hit
+		carve<float4>(z, P), carve<float4>(z, P);
+		carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
+		carve<int32_t>(z, P);
+		carve<unsigned>(z, 64);
+		carve<unsigned long long>(z, 8);
+		need = (size_t)z;
+	}
+	cudaStream_t s = sc->stream;
+	if (need > sc->ws_bytes) {
+		if (sc->ws) cudaFree(sc->ws);
+		sc->ws = nullptr;
+		sc->ws_bytes = 0;
+		if (are_status st = cuda_status(cudaMalloc(&sc->ws, need), "cudaMalloc(workspace)")) return st;
+		sc->ws_bytes = need;
+	}
+	size_t item_need = (size_t)W.n_items * 2 * sizeof(float4) + 2 * (size_t)W.npix * 3 * sizeof(float);
+	if (item_need > sc->items_bytes) {
+		if (sc->items) cudaFree(sc->items);
+		sc->items = nullptr;
+		sc->items_bytes = 0;
+		if (are_status st = cuda_status(cudaMalloc(&sc->items, item_need), "cudaMalloc(work items)")) return st;
+		sc->items_bytes = item_need;
+	}
+	{
+		char *z = (char *)sc->ws;
+		for (int q = 0; q < 2; ++q) W.qo[q] = carve<float4>(z, P), W.qd[q] = carve<float4>(z, P);
+		W.hit = carve<float4>(z, P);
+		W.st0 = carve<float4>(z, P), W.st1 = carve<float4>(z, P);
+		W.acc_s = carve<float4>(z, P), W.acc_c = carve<float4>(z, P), W.acc_q = carve<float4>(z, P);
+		W.term = carve<int32_t>(z, P);
+		W.cnt = carve<unsigned>(z, 64);
+		W.stat = carve<unsigned long long>(z, 8);
+		W.item_s = (float4 *)sc->items;
+		W.item_q = W.item_s + W.n_items;
+	}
+	float *d_rgb = (float *)(W.item_q + W.n_items);
+	float *d_var = d_rgb + 3 * (size_t)W.npix;
+	const bool dev_out = (p.flags & ARE_FLAG_DEVICE_OUTPUT) != 0;
+
+	cudaEvent_t ev0, ev1;
+	cudaEventCreate(&ev0);
+	cudaEventCreate(&ev1);
+	std::vector<cudaEvent_t> kev(4 * GRAPH_ITERS);
+	for (auto &e : kev) cudaEventCreate(&e);
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	are_status st = ARE_OK;
+	int64_t iterations = 0;
+	int64_t launches[4] = { 0, 0, 0, 0 };
+	double kms[4] = { 0.0, 0.0, 0.0, 0.0 };
+
+	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
+	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
+	const int g_gen = grid_for((const void *)k_generate, sc->n_sms);
+	const DevScene S = sc->dev;
+
+	unsigned init[8] = { (unsigned)std::min<int64_t>(P, W.n_items), 0u, 0u, (unsigned)std::min<int64_t>(P, W.n_items),
+		0u, 0u, 0u, 0u };
+	cudaEventRecord(ev0, s);
+	st = cuda_status(cudaMemcpyAsync(W.cnt, init, sizeof init, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(counters)");
+	if (!st) st = cuda_status(cudaMemsetAsync(W.stat, 0, 8 * sizeof(unsigned long long), s), "cudaMemsetAsync(stats)");
+	if (!st) {
+		k_init<<<grid_for((const void *)k_init, sc->n_sms), BLOCK, 0, s>>>(W, (int)init[0]);
+		++launches[ARE_KERNEL_OTHER];
+		st = cuda_status(cudaGetLastError(), "k_init launch");
+	}
+	// capture GRAPH_ITERS iterations, each bracketed by timing events
+	if (!st) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+	if (!st) {
+		for (int it = 0; it < GRAPH_ITERS; ++it) {
+			int par = it & 1;
+			cudaEventRecord(kev[4 * it + 0], s);
+			k_intersect<<<g_int, BLOCK, 0, s>>>(S, W, par);
+			cudaEventRecord(kev[4 * it + 1], s);
+			k_shade<<<g_sh, BLOCK, 0, s>>>(S, W, par);
+			cudaEventRecord(kev[4 * it + 2], s);
+			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
+			cudaEventRecord(kev[4 * it + 3], s);
+		}
+		st = cuda_status(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
+	}
+	if (!st) st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+	// run until no ray is queued; counters are read back one launch behind
+	const int64_t max_launches = (int64_t)(W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk + 16;
+	int64_t g = 0;
+	while (!st) {
+		st = cuda_status(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+		if (st) break;
+		cudaMemcpyAsync(sc->host_counters, W.cnt, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+		st = cuda_status(cudaStreamSynchronize(s), "render iteration");
+		if (st) break;
+		++g;
+		iterations += GRAPH_ITERS;
+		for (int it = 0; it < GRAPH_ITERS; ++it) {
+			for (int k = 0; k < 3; ++k) {
+				float ms = 0.f;
+				cudaEventElapsedTime(&ms, kev[4 * it + k], kev[4 * it + k + 1]);
+				kms[k] += ms;
+				++launches[k];
+			}
+		}
+		if (sc->host_counters[0] == 0) break;  // next iteration's input queue is empty
+		if (g > max_launches) {
+			set_error("render did not converge");
+			st = ARE_ERR_INTERNAL;
+		}
+	}
+	if (!st) {
+		k_resolve<<<std::max(1, std::min(4096, (W.npix + BLOCK - 1) / BLOCK)), BLOCK, 0, s>>>(
+			W, dev_out ? rgb : d_rgb, var ? (dev_out ? var : d_var) : nullptr, (p.flags & ARE_FLAG_CLAMP_OUTPUT) != 0);
+		++launches[ARE_KERNEL_OTHER];
+		st = cuda_status(cudaGetLastError(), "k_resolve launch");
+	}
+	cudaEventRecord(ev1, s);
+	unsigned long long hstat[2] = { 0, 0 };
+	unsigned herr = 0;
+	if (!st) {
+		cudaMemcpyAsync(hstat, W.stat, sizeof hstat, cudaMemcpyDeviceToHost, s);
+		cudaMemcpyAsync(&herr, W.cnt + 4, sizeof herr, cudaMemcpyDeviceToHost, s);
+		if (!dev_out) {
+			cudaMemcpyAsync(rgb, d_rgb, 3 * sizeof(float) * W.npix, cudaMemcpyDeviceToHost, s);
+			if (var) cudaMemcpyAsync(var, d_var, 3 * sizeof(float) * W.npix, cudaMemcpyDeviceToHost, s);
+		}
+		st = cuda_status(cudaStreamSynchronize(s), "render");
+	}
+	float total_ms = 0.f;
+	cudaEventElapsedTime(&total_ms, ev0, ev1);
+	if (exec) cudaGraphExecDestroy(exec);
+	if (graph) cudaGraphDestroy(graph);
+	for (auto &e : kev) cudaEventDestroy(e);
+	cudaEventDestroy(ev0);
+	cudaEventDestroy(ev1);
+	if (!st && herr) {
+		set_error("device error word " + std::to_string(herr));
+		st = ARE_ERR_INTERNAL;
+	}
+	if (stats) {
+		stats->samples = (int64_t)hstat[1];
+		stats->segments = (int64_t)hstat[0];
+		stats->iterations = iterations;
+		stats->device_ms = total_ms;
+		for (int k = 0; k < 4; ++k) stats->kernel_ms[k] = kms[k], stats->kernel_launches[k] = launches[k];
+		stats->error_word = (int32_t)herr;
+	}
+	return st;
+}
+
+are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms) {
+	if (!sc) return bad("null scene");
+	if (n < 0) return bad("negative ray count");
+	if (n == 0) {
+		if (ms) *ms = 0.f;
+		return ARE_OK;
+	}
+	if (!rays || !hits) return bad("null rays or hits");
+	cudaSetDevice(sc->device);
+	cudaStream_t s = sc->stream;
+	const float4 *d_rays = (const float4 *)rays;
+	float4 *d_hits = (float4 *)hits;
+	void *tmp = nullptr;
+	are_status st = ARE_OK;
+	if (!device_ptrs) {
+		st = cuda_status(cudaMalloc(&tmp, (size_t)n * 48 + 256), "cudaMalloc(intersect)");
+		if (st) return st;
+		d_rays = (const float4 *)tmp;
+		d_hits = (float4 *)((char *)tmp + (size_t)n * 32);
+		st = cuda_status(cudaMemcpyAsync((void *)d_rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, s), "H2D rays");
+	}
+	unsigned *err_word = nullptr;
+	if (!st) st = cuda_status(cudaMallocAsync((void **)&err_word, sizeof(unsigned), s), "cudaMallocAsync");
+	if (!st) st = cuda_status(cudaMemsetAsync(err_word, 0, sizeof(unsigned), s), "memset");
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	if (!st) {
+		int grid = grid_for((const void *)k_intersect_batch, sc->n_sms);
+		grid = (int)std::min<int64_t>(grid, (n + BLOCK - 1) / BLOCK);
+		cudaEventRecord(e0, s);
+		k_intersect_batch<<<grid, BLOCK, 0, s>>>(sc->dev, d_rays, n, d_hits, err_word);
+		cudaEventRecord(e1, s);
+		st = cuda_status(cudaGetLastError(), "k_intersect_batch launch");
+	}
+	unsigned herr = 0;
+	if (!st) {
+		if (!device_ptrs)
+			st = cuda_status(cudaMemcpyAsync(hits, d_hits, (size_t)n * 16, cudaMemcpyDeviceToHost, s), "D2H hits");
+		cudaMemcpyAsync(&herr, err_word, sizeof herr, cudaMemcpyDeviceToHost, s);
+		if (!st) st = cuda_status(cudaStreamSynchronize(s), "intersect");
+	}
+	if (ms) {
+		float t = 0.f;
+		cudaEventElapsedTime(&t, e0, e1);
+		*ms = t;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if (err_word) cudaFreeAsync(err_word, s);
+	if (tmp) {
+		cudaStreamSynchronize(s);
+		cudaFree(tmp);
+	}
+	if (!st && herr) {
+		set_error("device error word " + std::to_string(herr));
+		st = ARE_ERR_INTERNAL;
+	}
+	return st;
+}
+
+}  // namespace are_core

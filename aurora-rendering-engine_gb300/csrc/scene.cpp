@@ -1,0 +1,246 @@
+// scene.cpp — are_scene_create: validate a flat scene descriptor, build the
+// BVH on the host and upload the SoA primitive records to the device.
+//
+// Replaces the construction of rt.cpp's Scene (experiments/rt.cpp:146-186)
+// and of an are::ObjectSet of are::Triangle objects.  Validation mirrors the
+// reference's error behaviour where it has one: are::Triangle's constructor
+// rejects null materials/textures, zero edge vectors and collinear edges
+// (src/object/triangle.cpp:9-46); here those become ARE_ERR_INVALID_ARGUMENT.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bvh.h"
+#include "scene.h"
+
+namespace are_core {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+const char *last_error() { return g_err.c_str(); }
+
+are_status cuda_status(cudaError_t e, const char *what) {
+	if (e == cudaSuccess) return ARE_OK;
+	set_error(std::string(what) + ": " + cudaGetErrorString(e));
+	if (e == cudaErrorMemoryAllocation) return ARE_ERR_OUT_OF_MEMORY;
+	if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return ARE_ERR_NO_DEVICE;
+	return ARE_ERR_CUDA;
+}
+
+namespace {
+
+are_status invalid(const std::string &msg) {
+	set_error(msg);
+	return ARE_ERR_INVALID_ARGUMENT;
+}
+
+bool finite3(const float *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+// are::Vec3::near_zero (src/basic/vec3.cpp:143-146): every |component| < 1e-8
+bool near_zero(const double *v) { return std::fabs(v[0]) < 1e-8 && std::fabs(v[1]) < 1e-8 && std::fabs(v[2]) < 1e-8; }
+
+void cross_d(const double *a, const double *b, double *c) {
+	c[0] = a[1] * b[2] - a[2] * b[1];
+	c[1] = a[2] * b[0] - a[0] * b[2];
+	c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+are_status validate(const are_scene_desc *d) {
+	if (!d) return invalid("scene descriptor is null");
+	if (d->n_spheres < 0 || d->n_quads < 0 || d->n_triangles < 0 || d->n_materials < 0 || d->n_textures < 0 ||
+		d->n_texels < 0)
+		return invalid("negative count in scene descriptor");
+	if ((d->n_spheres && (!d->spheres || !d->sphere_mat)) || (d->n_quads && (!d->quads || !d->quad_mat)) ||
+		(d->n_triangles && (!d->triangles || !d->triangle_mat)) || (d->n_materials && !d->materials) ||
+		(d->n_textures && !d->textures) || (d->n_texels && !d->texels))
+		return invalid("null array with a non-zero count in scene descriptor");
+	int64_t total = (int64_t)d->n_spheres + d->n_quads + d->n_triangles;
+	if (total > (int64_t)INT32_MAX / 4) return invalid("too many primitives");
+	if (d->background != ARE_BG_CONSTANT && d->background != ARE_BG_SKY_GRADIENT) return invalid("unknown background");
+	if (d->triangle_test != ARE_TRI_REFERENCE_MT && d->triangle_test != ARE_TRI_WATERTIGHT)
+		return invalid("unknown triangle test");
+	for (int32_t i = 0; i < d->n_textures; ++i) {
+		const are_texture &t = d->textures[i];
+		if (t.type < ARE_TEX_SOLID || t.type > ARE_TEX_IMAGE) return invalid("texture " + std::to_string(i) + ": unknown type");
+		if (t.mapping != ARE_MAP_SURFACE_UV && t.mapping != ARE_MAP_SPHERICAL)
+			return invalid("texture " + std::to_string(i) + ": unknown mapping");
+		if (t.type == ARE_TEX_IMAGE) {
+			// are::Texture rejects non-positive sizes (src/texture.cpp:52-55)
+			if (t.width <= 0 || t.height <= 0) return invalid("texture " + std::to_string(i) + ": width and height must be positive");
+			if (t.texel_offset < 0 || (int64_t)t.texel_offset + (int64_t)t.width * t.height > d->n_texels)
+				return invalid("texture " + std::to_string(i) + ": texel range outside texels[]");
+		}
+	}
+	for (int32_t i = 0; i < d->n_materials; ++i) {
+		const are_material &m = d->materials[i];
+		if (m.type < ARE_MAT_LAMBERTIAN || m.type > ARE_MAT_DIFFUSE_LIGHT)
+			return invalid("material " + std::to_string(i) + ": unknown type");
+		if (m.texture < -1 || m.texture >= d->n_textures)
+			return invalid("material " + std::to_string(i) + ": texture index out of range");
+		if (m.type == ARE_MAT_DIELECTRIC && !(m.ior > 0.0f)) return invalid("material " + std::to_string(i) + ": ior must be > 0");
+		if (m.type == ARE_MAT_METAL && !(m.fuzz >= 0.0f)) return invalid("material " + std::to_string(i) + ": fuzz must be >= 0");
+	}
+	auto check_mat = [&](int32_t m, const char *what, int32_t i) -> are_status {
+		if (m < 0 || m >= d->n_materials)
+			return invalid(std::string(what) + " " + std::to_string(i) + ": material index out of range");
+		return ARE_OK;
+	};
+	for (int32_t i = 0; i < d->n_spheres; ++i) {
+		const float *s = d->spheres + 4 * (size_t)i;
+		if (!finite3(s) || !(s[3] > 0.0f) || !std::isfinite(s[3]))
+			return invalid("sphere " + std::to_string(i) + ": centre must be finite and radius > 0");
+		if (are_status st = check_mat(d->sphere_mat[i], "sphere", i)) return st;
+	}
+	for (int32_t i = 0; i < d->n_quads; ++i) {
+		const float *q = d->quads + 9 * (size_t)i;
+		if (!finite3(q) || !finite3(q + 3) || !finite3(q + 6)) return invalid("quad " + std::to_string(i) + ": non-finite");
+		double u[3] = { q[3], q[4], q[5] }, v[3] = { q[6], q[7], q[8] }, c[3];
+		cross_d(u, v, c);
+		if (near_zero(u) || near_zero(v) || near_zero(c)) return invalid("quad " + std::to_string(i) + ": degenerate edges");
+		if (are_status st = check_mat(d->quad_mat[i], "quad", i)) return st;
+	}
+	for (int32_t i = 0; i < d->n_triangles; ++i) {
+		const float *t = d->triangles + 9 * (size_t)i;
+		if (!finite3(t) || !finite3(t + 3) || !finite3(t + 6))
+			return invalid("triangle " + std::to_string(i) + ": non-finite vertex");
+		double u[3], v[3], c[3];
+		for (int k = 0; k < 3; ++k) u[k] = (double)t[3 + k] - t[k], v[k] = (double)t[6 + k] - t[k];
+		cross_d(u, v, c);
+		// src/object/triangle.cpp:21-36: zero or collinear edge vectors throw
+		if (near_zero(u) || near_zero(v)) return invalid("triangle " + std::to_string(i) + ": edge vector is zero");
+		if (near_zero(c)) return invalid("triangle " + std::to_string(i) + ": edge vectors are collinear");
+		if (are_status st = check_mat(d->triangle_mat[i], "triangle", i)) return st;
+	}
+	return ARE_OK;
+}
+
+template <class T>
+are_status upload(are_scene *sc, const T *src, size_t count, const T **dst) {
+	if (count == 0) {
+		*dst = nullptr;
+		return ARE_OK;
+	}
+	void *p = nullptr;
+	if (are_status st = cuda_status(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc(scene)")) return st;
+	sc->allocations.push_back(p);
+	if (are_status st = cuda_status(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy(scene)"))
+		return st;
+	*dst = (const T *)p;
+	return ARE_OK;
+}
+
+}  // namespace
+
+are_status scene_create(const are_scene_desc *d, are_scene **out) {
+	if (!out) return invalid("output handle pointer is null");
+	*out = nullptr;
+	if (are_status st = validate(d)) return st;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+		cudaGetLastError();
+		set_error("no CUDA device");
+		return ARE_ERR_NO_DEVICE;
+	}
+	const int32_t ns = d->n_spheres, nq = d->n_quads, nt = d->n_triangles;
+	const int32_t n = ns + nq + nt;
+
+	// primitive bounds in double
+	std::vector<PrimBox> boxes((size_t)n);
+	for (int32_t i = 0; i < ns; ++i) {
+		const float *s = d->spheres + 4 * (size_t)i;
+		for (int k = 0; k < 3; ++k) boxes[i].lo[k] = (double)s[k] - s[3], boxes[i].hi[k] = (double)s[k] + s[3];
+	}
+	for (int32_t i = 0; i < nq; ++i) {
+		const float *q = d->quads + 9 * (size_t)i;
+		PrimBox &b = boxes[ns + i];
+		for (int k = 0; k < 3; ++k) {
+			double c0 = q[k], c1 = (double)q[k] + q[3 + k], c2 = (double)q[k] + q[6 + k], c3 = c1 + q[6 + k];
+			b.lo[k] = std::fmin(std::fmin(c0, c1), std::fmin(c2, c3));
+			b.hi[k] = std::fmax(std::fmax(c0, c1), std::fmax(c2, c3));
+		}
+	}
+	for (int32_t i = 0; i < nt; ++i) {
+		const float *t = d->triangles + 9 * (size_t)i;
+		PrimBox &b = boxes[ns + nq + i];
+		for (int k = 0; k < 3; ++k) {
+			b.lo[k] = std::fmin(std::fmin((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
+			b.hi[k] = std::fmax(std::fmax((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
+		}
+	}
+	BvhResult bvh = build_bvh(boxes, d->bvh_leaf_size);
+
+	// SoA records in leaf order
+	std::vector<float> prims(12 * (size_t)std::max(n, 1), 0.0f);
+	std::vector<int32_t> gid((size_t)std::max(n, 1), 0), mat((size_t)std::max(n, 1), 0);
+	std::vector<float> tri_uv;
+	if (d->triangle_uv && nt) tri_uv.assign(6 * (size_t)n, 0.0f);
+	for (int32_t j = 0; j < n; ++j) {
+		int32_t g = bvh.order[j];
+		float *o = &prims[12 * (size_t)j];
+		gid[j] = g;
+		if (g < ns) {
+			std::memcpy(o, d->spheres + 4 * (size_t)g, 16);
+			mat[j] = d->sphere_mat[g];
+		} else if (g < ns + nq) {
+			const float *q = d->quads + 9 * (size_t)(g - ns);
+			for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, q + 3 * r, 12);
+			o[3] = PRIM_TAG_QUAD;
+			mat[j] = d->quad_mat[g - ns];
+		} else {
+			const float *t = d->triangles + 9 * (size_t)(g - ns - nq);
+			for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, t + 3 * r, 12);
+			o[3] = PRIM_TAG_TRI;
+			mat[j] = d->triangle_mat[g - ns - nq];
+			if (!tri_uv.empty()) std::memcpy(&tri_uv[6 * (size_t)j], d->triangle_uv + 6 * (size_t)(g - ns - nq), 24);
+		}
+	}
+
+	are_scene *sc = new are_scene();
+	cudaGetDevice(&sc->device);
+	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
+	are_status st = ARE_OK;
+	DevScene &S = sc->dev;
+	const float4 *pp = nullptr, *np = nullptr;
+	if (!st) st = upload(sc, (const float4 *)prims.data(), prims.size() / 4, &pp);
+	if (!st) st = upload(sc, gid.data(), gid.size(), &S.prim_gid);
+	if (!st) st = upload(sc, mat.data(), mat.size(), &S.prim_mat);
+	if (!st) st = upload(sc, tri_uv.data(), tri_uv.size(), &S.tri_uv);
+	if (!st) st = upload(sc, (const float4 *)bvh.nodes.data(), bvh.nodes.size() / 4, &np);
+	if (!st) st = upload(sc, (const DevMaterial *)d->materials, (size_t)d->n_materials, &S.mats);
+	if (!st) st = upload(sc, (const DevTexture *)d->textures, (size_t)d->n_textures, &S.texs);
+	if (!st) st = upload(sc, d->texels, 3 * (size_t)d->n_texels, &S.texels);
+	if (!st) st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	if (!st) st = cuda_status(cudaMallocHost((void **)&sc->host_counters, 64 * sizeof(unsigned)), "cudaMallocHost");
+	if (st) {
+		delete sc;
+		return st;
+	}
+	S.prims = pp;
+	S.nodes = np;
+	S.n_prims = n;
+	S.n_nodes = bvh.n_nodes;
+	S.n_materials = d->n_materials;
+	S.n_textures = d->n_textures;
+	S.background = d->background;
+	S.triangle_test = d->triangle_test;
+	for (int k = 0; k < 3; ++k) S.bg_a[k] = d->bg_a[k], S.bg_b[k] = d->bg_b[k];
+	S.box_pad = bvh.box_pad;
+	sc->n_prims = n;
+	sc->n_nodes = bvh.n_nodes;
+	sc->max_leaf = bvh.max_leaf;
+	sc->depth = bvh.depth;
+	*out = sc;
+	return ARE_OK;
+}
+
+}  // namespace are_core
+
+are_scene::~are_scene() {
+	if (stream) cudaStreamSynchronize(stream);
+	for (void *p : allocations) cudaFree(p);
+	if (ws) cudaFree(ws);
+	if (items) cudaFree(items);
+	if (host_counters) cudaFreeHost(host_counters);
+	if (stream) cudaStreamDestroy(stream);
+}

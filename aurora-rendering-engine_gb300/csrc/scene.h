@@ -1,0 +1,46 @@
+// scene.h — host-side owner of a device-resident scene and its render
+// workspace (the opaque are_scene of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "core.h"
+
+struct are_scene {
+	are_core::DevScene dev{};
+	int device = 0;
+	int n_sms = 0;
+	int64_t n_prims = 0, n_nodes = 0;
+	int32_t max_leaf = 0, depth = 0;
+	std::vector<void *> allocations;  // device buffers owned by the scene
+	cudaStream_t stream = nullptr;
+
+	// cached wavefront workspace (grown on demand)
+	void *ws = nullptr;
+	size_t ws_bytes = 0;
+	void *items = nullptr;
+	size_t items_bytes = 0;
+	unsigned *host_counters = nullptr;  // pinned
+
+	~are_scene();
+};
+
+namespace are_core {
+
+// thread-local last error message for are_last_error()
+void set_error(const std::string &msg);
+const char *last_error();
+
+// CUDA call guard: records a message and returns ARE_ERR_CUDA / ARE_ERR_OUT_OF_MEMORY
+are_status cuda_status(cudaError_t e, const char *what);
+
+are_status scene_create(const are_scene_desc *desc, are_scene **out);
+are_status render(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
+	are_render_stats *stats);
+are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms);
+
+}  // namespace are_core

@@ -1,0 +1,295 @@
+// traverse.cuh — closest-hit queries on the device.
+//
+// Primitive tests use __fadd_rn/__fsub_rn/__fmul_rn/__fdiv_rn/__fsqrt_rn so
+// no multiply-add is ever contracted: each operation rounds exactly as the
+// reference's FP32 code does on the host (rt.cpp:123-138 for the triangle
+// test), which makes closest-hit ids, t, u and v bit-identical to the CPU
+// restatement.  Box tests are only culling and are free to use FMA: node
+// boxes are padded (core.h) so they never reject a primitive hit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "core.h"
+
+namespace are_core {
+
+struct f3 {
+	float x, y, z;
+};
+
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{ x, y, z }; }
+__device__ __forceinline__ f3 ld3(float4 v) { return f3{ v.x, v.y, v.z }; }
+__device__ __forceinline__ f3 rsub(f3 a, f3 b) {
+	return f3{ __fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z) };
+}
+__device__ __forceinline__ f3 radd(f3 a, f3 b) {
+	return f3{ __fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z) };
+}
+__device__ __forceinline__ f3 rscl(f3 a, float s) {
+	return f3{ __fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s) };
+}
+// ((ax*bx + ay*by) + az*bz), each step rounded
+__device__ __forceinline__ float rdot(f3 a, f3 b) {
+	return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ f3 rcross(f3 a, f3 b) {
+	return f3{ __fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+		__fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)) };
+}
+
+// Sphere: discriminant a (r^2 - |l|^2) with l = f + (b/a) d (Haines et al.,
+// Ray Tracing Gems 2019, ch. 7), roots c/q and q/a.  New primitive.
+__device__ __forceinline__ bool hit_sphere(float4 s0, f3 o, f3 d, float tmin, float tmax, float &tout) {
+	f3 c = ld3(s0);
+	float r = s0.w;
+	f3 f = rsub(o, c);
+	float a = rdot(d, d);
+	float b = -rdot(f, d);
+	float s = __fdiv_rn(b, a);
+	f3 l = radd(f, rscl(d, s));
+	float r2 = __fmul_rn(r, r);
+	float disc = __fmul_rn(a, __fsub_rn(r2, rdot(l, l)));
+	if (!(disc >= 0.0f)) return false;
+	float cc = __fsub_rn(rdot(f, f), r2);
+	float sq = __fsqrt_rn(disc);
+	float q = __fadd_rn(b, copysignf(sq, b));
+	float t0 = __fdiv_rn(cc, q);
+	float t1 = __fdiv_rn(q, a);
+	float tn = t0 < t1 ? t0 : t1;
+	float tf = t0 < t1 ? t1 : t0;
+	if (tn > tmin && tn < tmax) {
+		tout = tn;
+		return true;
+	}
+	if (tf > tmin && tf < tmax) {
+		tout = tf;
+		return true;
+	}
+	return false;
+}
+
+// Quad (Q, u, v): plane hit (src/basic/plane.cpp:13-27), then the planar
+// coordinates alpha, beta in [0,1]^2.  New primitive.
+__device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmin, float tmax, float &tout,
+	float &uo, float &vo) {
+	f3 n = rcross(u, v);
+	float denom = rdot(n, d);
+	if (denom == 0.0f) return false;
+	float t = __fdiv_rn(rdot(n, rsub(Q, o)), denom);
+	if (!(t > tmin && t < tmax)) return false;
+	f3 p = rsub(radd(o, rscl(d, t)), Q);
+	float nn = rdot(n, n);
+	float al = __fdiv_rn(rdot(n, rcross(p, v)), nn);
+	float be = __fdiv_rn(rdot(n, rcross(u, p)), nn);
+	if (!(al >= 0.0f && al <= 1.0f && be >= 0.0f && be <= 1.0f)) return false;
+	tout = t;
+	uo = al;
+	vo = be;
+	return true;
+}
+
+// Triangle, Möller–Trumbore exactly as rt.cpp Tri::intersect (rt.cpp:123-138),
+// with EPS = 1e-5f (rt.cpp:15) as the parallel threshold and the reference's
+// NaN-passing comparisons.
+__device__ __forceinline__ bool hit_tri_mt(f3 v0, f3 v1, f3 v2, f3 o, f3 d, float tmin, float tmax, float &tout,
+	float &uo, float &vo) {
+	f3 e1 = rsub(v1, v0), e2 = rsub(v2, v0), h = rcross(d, e2), s = rsub(o, v0);
+	float a = rdot(e1, h);
+	if (fabsf(a) < 1e-5f) return false;
+	float f = __frcp_rn(a);
+	float u = __fmul_rn(f, rdot(s, h));
+	if (u < 0.0f || u > 1.0f) return false;
+	f3 q = rcross(s, e1);
+	float v = __fmul_rn(f, rdot(d, q));
+	if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
+	float t = __fmul_rn(f, rdot(e2, q));
+	if (!(t > tmin && t < tmax)) return false;
+	tout = t;
+	uo = u;
+	vo = v;
+	return true;
+}
+
+// Triangle, watertight (Woop, Benthin, Wald, JCGT 2013).
+__device__ __forceinline__ bool hit_tri_wt(f3 v0, f3 v1, f3 v2, f3 o, f3 d, float tmin, float tmax, float &tout,
+	float &uo, float &vo) {
+	float dd[3] = { d.x, d.y, d.z };
+	int kz = 0;
+	if (fabsf(dd[1]) > fabsf(dd[kz])) kz = 1;
+	if (fabsf(dd[2]) > fabsf(dd[kz])) kz = 2;
+	int kx = kz == 2 ? 0 : kz + 1;
+	int ky = kx == 2 ? 0 : kx + 1;
+	if (dd[kz] < 0.0f) {
+		int tmp = kx;
+		kx = ky;
+		ky = tmp;
+	}
+	float dkz = dd[kz];
+	float Sx = __fdiv_rn(dd[kx], dkz), Sy = __fdiv_rn(dd[ky], dkz), Sz = __frcp_rn(dkz);
+	f3 A = rsub(v0, o), B = rsub(v1, o), C = rsub(v2, o);
+	float Aa[3] = { A.x, A.y, A.z }, Ba[3] = { B.x, B.y, B.z }, Ca[3] = { C.x, C.y, C.z };
+	float Ax = __fsub_rn(Aa[kx], __fmul_rn(Sx, Aa[kz])), Ay = __fsub_rn(Aa[ky], __fmul_rn(Sy, Aa[kz]));
+	float Bx = __fsub_rn(Ba[kx], __fmul_rn(Sx, Ba[kz])), By = __fsub_rn(Ba[ky], __fmul_rn(Sy, Ba[kz]));
+	float Cx = __fsub_rn(Ca[kx], __fmul_rn(Sx, Ca[kz])), Cy = __fsub_rn(Ca[ky], __fmul_rn(Sy, Ca[kz]));
+	float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+	float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+	float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+	if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+	float det = __fadd_rn(__fadd_rn(U, V), W);
+	if (det == 0.0f) return false;
+	float Az = __fmul_rn(Sz, Aa[kz]), Bz = __fmul_rn(Sz, Ba[kz]), Cz = __fmul_rn(Sz, Ca[kz]);
+	float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+	float rcp = __frcp_rn(det);
+	float t = __fmul_rn(T, rcp);
+	if (!(t > tmin && t < tmax)) return false;
+	tout = t;
+	uo = __fmul_rn(V, rcp);
+	vo = __fmul_rn(W, rcp);
+	return true;
+}
+
+struct Hit {
+	float t;
+	int32_t leaf;  // leaf-order primitive index, -1 on a miss
+	int32_t gid;   // global id
+	float u, v;
+};
+
+__device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
+
+// Closest hit with the (t, global id) order.  `snodes` holds the first
+// `n_snodes` nodes in shared memory.  err receives ERR_* bits.
+__device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
+	f3 d, float tmin, float tmax, uint32_t &err) {
+	Hit best;
+	best.t = __int_as_float(0x7f800000);
+	best.leaf = -1;
+	best.gid = 0x7fffffff;
+	best.u = best.v = 0.0f;
+	// slab setup: exact zeros become a tiny value so no 0 * inf appears
+	float dx = d.x != 0.0f ? d.x : copysignf(1e-20f, d.x);
+	float dy = d.y != 0.0f ? d.y : copysignf(1e-20f, d.y);
+	float dz = d.z != 0.0f ? d.z : copysignf(1e-20f, d.z);
+	float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
+	float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+	const float4 *__restrict__ G = S.nodes;
+	const int32_t tri_wt = S.triangle_test;
+	if (S.n_prims == 0) return best;
+
+	int2 stack[MAX_STACK];
+	int sp = 0;
+	// current node (a, b): start with the root's
+	float4 r1 = n_snodes > 0 ? snodes[1] : ldg4(G + 1);
+	float4 r0 = n_snodes > 0 ? snodes[0] : ldg4(G + 0);
+	int a = __float_as_int(r0.w), b = __float_as_int(r1.w);
+	{
+		// root box test
+		float t0x = fmaf(r0.x, ix, ox), t1x = fmaf(r1.x, ix, ox);
+		float t0y = fmaf(r0.y, iy, oy), t1y = fmaf(r1.y, iy, oy);
+		float t0z = fmaf(r0.z, iz, oz), t1z = fmaf(r1.z, iz, oz);
+		float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+		float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax * 1.0000039f));
+		if (!(lo <= hi)) return best;
+	}
+	while (true) {
+		if (b == 0) {
+			// interior: test both children (one 64-byte line)
+			int c = a;
+			float4 c00, c01, c10, c11;
+			if (c + 1 < n_snodes) {
+				c00 = snodes[2 * c];
+				c01 = snodes[2 * c + 1];
+				c10 = snodes[2 * c + 2];
+				c11 = snodes[2 * c + 3];
+			} else {
+				c00 = ldg4(G + 2 * c);
+				c01 = ldg4(G + 2 * c + 1);
+				c10 = ldg4(G + 2 * c + 2);
+				c11 = ldg4(G + 2 * c + 3);
+			}
+			float bt = fminf(best.t * 1.0000039f, tmax * 1.0000039f);
+			float l0, l1;
+			bool h0, h1;
+			{
+				float t0x = fmaf(c00.x, ix, ox), t1x = fmaf(c01.x, ix, ox);
+				float t0y = fmaf(c00.y, iy, oy), t1y = fmaf(c01.y, iy, oy);
+				float t0z = fmaf(c00.z, iz, oz), t1z = fmaf(c01.z, iz, oz);
+				l0 = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+				float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+				h0 = l0 <= hi;
+			}
+			{
+				float t0x = fmaf(c10.x, ix, ox), t1x = fmaf(c11.x, ix, ox);
+				float t0y = fmaf(c10.y, iy, oy), t1y = fmaf(c11.y, iy, oy);
+				float t0z = fmaf(c10.z, iz, oz), t1z = fmaf(c11.z, iz, oz);
+				l1 = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+				float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+				h1 = l1 <= hi;
+			}
+			if (h0 && h1) {
+				int2 nearn = make_int2(__float_as_int(c00.w), __float_as_int(c01.w));
+				int2 farn = make_int2(__float_as_int(c10.w), __float_as_int(c11.w));
+				if (l1 < l0) {
+					int2 t = nearn;
+					nearn = farn;
+					farn = t;
+				}
+				if (sp < MAX_STACK) {
+					stack[sp++] = farn;
+				} else {
+					err |= ERR_STACK_OVERFLOW;
+				}
+				a = nearn.x;
+				b = nearn.y;
+				continue;
+			}
+			if (h0) {
+				a = __float_as_int(c00.w);
+				b = __float_as_int(c01.w);
+				continue;
+			}
+			if (h1) {
+				a = __float_as_int(c10.w);
+				b = __float_as_int(c11.w);
+				continue;
+			}
+		} else {
+			// leaf: primitives [a, a + b)
+			for (int i = a; i < a + b; ++i) {
+				const float4 *P = S.prims + 3 * (size_t)i;
+				float4 p0 = ldg4(P);
+				float t, u = 0.0f, v = 0.0f;
+				bool h;
+				if (p0.w > 0.0f) {
+					h = hit_sphere(p0, o, d, tmin, tmax, t);
+				} else {
+					float4 p1 = ldg4(P + 1), p2 = ldg4(P + 2);
+					if (p0.w == PRIM_TAG_QUAD)
+						h = hit_quad(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+					else if (tri_wt)
+						h = hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+					else
+						h = hit_tri_mt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+				}
+				if (h && t <= best.t) {
+					int32_t gid = __ldg(S.prim_gid + i);
+					if (t < best.t || gid < best.gid) {
+						best.t = t;
+						best.leaf = i;
+						best.gid = gid;
+						best.u = u;
+						best.v = v;
+					}
+				}
+			}
+		}
+		if (sp == 0) break;
+		int2 nx = stack[--sp];
+		a = nx.x;
+		b = nx.y;
+	}
+	return best;
+}
+
+}  // namespace are_core

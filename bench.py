@@ -1,0 +1,307 @@
+"""Benchmark: samples/s of the per-pixel render loop on the Cornell-box workload.
+
+One step = one full frame of the Cornell box (600 x 600 pixels, 1024 samples
+per pixel, max depth 50, FP32) rendered by the CUDA core through its C ABI.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value: samples per second over the K timed steps, scene resident in HBM and
+  the image written to device memory; per-step CUDA-event time on the
+  render's stream, bracketed by a barrier and device synchronisation.
+* e2e: the same metric through the public entry points with host buffers:
+  are_scene_create from the host descriptor (BVH build + upload),
+  are_render to a host image, are_scene_destroy, every step.
+* roofline: the dominant kernel's algorithmic bytes per launch divided by its
+  average CUDA-event duration, against the measured HBM copy bandwidth.
+* cpu_baseline: the oracle's CPU port of the same estimator on this host's
+  cores, on a bounded sample of the same frame (fewer samples per pixel).
+* --impl reference: the reference's CPU implementation of the path (the
+  oracle port: the reference's rt.cpp cannot express this scene) on all host
+  cores, same metric and config, bounded sample per step.
+
+N > 1 (torchrun): every rank renders its own frame (replicas, weak scaling);
+value = all ranks' samples / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "aurora-rendering-engine_gb300"
+for _p in (str(REPO), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Msamples/s on 1 GB300 vs host CPU ref; equal-time relMSE, guided vs plain"
+UNIT = "Msamples/s"
+WORKLOAD = "cornell_box_600x600_1024spp_depth50"
+# algorithmic bytes of the wavefront's compulsory SoA traffic per path segment
+BYTES_INTERSECT = 32 + 16                    # ray record in, hit record out
+BYTES_SHADE = 32 + 16 + 32 + 32 + 32 + 4      # ray, hit, path state read + write, next ray, list index
+BYTES_GENERATE = 4 + 32 + 48 + 48 + 32 + 32   # list index, state read, accumulator read + write, state, camera ray
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_sample(scene, cam, par, budget_s: float, threads: int) -> dict:
+    """Oracle port on host cores over a bounded sample of the frame: all
+    pixels of a band of rows at reduced spp, sized to about budget_s."""
+    from oracle.orc import Oracle
+
+    orc = Oracle()
+    ctx = orc.prepare(scene)
+    probe = dict(par, spp=1)
+    rows = max(1, par["height"] // 20)
+    t = time.perf_counter()
+    _, _, st = orc.render(ctx, cam, probe, nthreads=threads, rows=(0, rows))
+    dt = max(time.perf_counter() - t, 1e-3)
+    per_sample = dt / max(1, st["samples"])
+    spp = max(1, min(par["spp"], int(budget_s / (per_sample * par["width"] * par["height"]))))
+    p = dict(par, spp=spp)
+    nrows = par["height"]
+    if spp == 1:
+        nrows = max(1, min(par["height"], int(budget_s / (per_sample * par["width"]))))
+    t = time.perf_counter()
+    _, _, st = orc.render(ctx, cam, p, nthreads=threads, rows=(0, nrows))
+    dt = time.perf_counter() - t
+    return {"value": st["samples"] / dt / 1e6, "seconds": dt, "samples": st["samples"], "spp": spp, "rows": nrows,
+            "segments": st["segments"]}
+
+
+def run_reference(args, rank, world) -> None:
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    if rank != 0:
+        return
+    import are_gb300 as are
+
+    scene, cam, par = are.build_config(are.CONFIG_CORNELL)
+    threads = os.cpu_count() or 1
+    budget = float(os.environ.get("ARE_REF_STEP_SECONDS", "8"))
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(scene, cam, dict(par, seed=1 + i), budget if i >= args.warmup else 2.0, threads)
+        if i >= args.warmup:
+            vals.append(r["value"])
+            info = r
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(info["seconds"] * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": 600, "height": 600, "spp": 1024, "max_depth": 50,
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{info['rows']} rows x 600 px x {info['spp']} spp of the frame per step "
+                                   f"(oracle/ C port of the estimator; rt.cpp has no quads or emission)"},
+        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp", type=int, default=1024)
+    ap.add_argument("--pool", type=int, default=0)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if pg:
+            pg.barrier()
+            pg.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    import are_gb300 as are
+
+    torch.cuda.set_device(local)
+    L = are.load()
+    scene_arrays, cam, par = are.build_config(are.CONFIG_CORNELL)
+    par = dict(par, spp=args.spp, pool_size=args.pool, chunk=args.chunk)
+    W, H = par["width"], par["height"]
+    samples_per_step = W * H * par["spp"]
+    sc = are.Scene(scene_arrays)
+    rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+
+    def step(seed):
+        return sc.render_device(cam, dict(par, seed=seed), rgb.data_ptr())
+
+    for i in range(args.warmup):
+        step(1000 + i)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    stats = []
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            stats.append(step(1 + i))
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    dev_ms = sum(s["device_ms"] for s in stats)
+    if pg:
+        t = torch.tensor([dev_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        pg.barrier()
+    torch.cuda.synchronize()
+    value = world * samples_per_step * args.steps / (dev_ms / 1e3) / 1e6
+
+    # kernel-level roofline over the same timed steps
+    tot = {k: sum(s["kernel_ms"][k] for s in stats) for k in are.KERNELS}
+    launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
+    segments = sum(s["segments"] for s in stats)
+    samples = sum(s["samples"] for s in stats)
+    algo = {"intersect": BYTES_INTERSECT * segments, "shade": BYTES_SHADE * segments,
+            "generate": BYTES_GENERATE * samples}
+    dom = max(("intersect", "shade", "generate"), key=lambda k: tot[k])
+    peaks = measured_peaks()
+    achieved = algo[dom] / (tot[dom] / 1e3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
+            "bytes_per_launch": round(algo[dom] / max(1, launches[dom])),
+            "avg_launch_us": round(tot[dom] * 1e3 / max(1, launches[dom]), 2),
+            "kernel_ms": {k: round(v, 2) for k, v in tot.items()},
+            "traffic": None}
+    prof = REPO / "profiles" / "traffic.json"
+    if prof.exists():
+        roof["traffic"] = json.loads(prof.read_text()).get(dom)
+
+    # end to end through the C ABI with host buffers
+    host_rgb = np.empty(W * H * 3, np.float32)
+    e2e_times = []
+    d, keep = are.desc_struct(scene_arrays)
+    import ctypes as C
+
+    cam_s = are.Camera.from_dict(cam)
+    for i in range(max(2, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = C.c_void_p()
+        are.check(L.are_scene_create(C.byref(d), C.byref(h)))
+        p = are.RenderParams.from_dict(dict(par, seed=77 + i))
+        st = are.RenderStats()
+        are.check(L.are_render(h, C.byref(cam_s), C.byref(p), host_rgb.ctypes.data, None, C.byref(st)))
+        L.are_scene_destroy(h)
+        e2e_times.append(time.perf_counter() - t0)
+    h2d = sum(a.nbytes for a in keep if hasattr(a, "nbytes"))
+    e2e = {"value": round(samples_per_step / statistics.median(e2e_times) / 1e6 * world, 3), "unit": UNIT,
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.nbytes)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r = cpu_sample(scene_arrays, cam, par, float(os.environ.get("ARE_CPU_SECONDS", "15")), threads)
+        cpu = {"value": round(r["value"], 4), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{r['rows']} rows x {W} px x {r['spp']} spp of the same frame ({r['seconds']:.1f} s)"}
+
+    if rank == 0:
+        gpu_launches = sum(sum(s["kernel_launches"].values()) for s in stats)
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
+                       "rr_depth": par["rr_depth"], "scene": "cornell box, 18 quads", "parallelism": f"replicas{world}",
+                       "l2": "flushed (256 MB write) between steps; path pool > L2"},
+            "segments_per_sample": round(segments / max(1, samples), 4),
+            "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
+            "wall_s": round(wall, 3),
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clk.summary(), "gpu_launches": gpu_launches,
+        }
+        print(json.dumps(line), flush=True)
+    sc.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

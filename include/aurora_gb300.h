@@ -1,0 +1,227 @@
+/*
+ * aurora_gb300.h — C ABI of the GB300 path-tracing core.
+ *
+ * This is the drop-in boundary for the reference's per-pixel render loop.
+ * The reference has no FFI of its own; the call it replaces is
+ *
+ *     void render(const Scene&, const Vec3& camPos, const Vec3& camTarget,
+ *                 const Vec3& camUp, float fov, Viewport& vp)
+ *
+ * in experiments/rt.cpp:337-374, which walks every pixel, builds the camera
+ * ray (rt.cpp:339-343,364-366), calls trace() (rt.cpp:251-334) and stores the
+ * clamped colour (rt.cpp:368-369).  The scene the reference renders is a
+ * caller-owned list of triangles with a material tag and a texture pointer
+ * each (rt.cpp:110-186); the library's scene types are are::ObjectSet /
+ * are::Triangle / are::Material / are::Texture (include/object/object_set.h:10-12,
+ * include/object/triangle.h:15-46, include/material/material.h:10-29,
+ * include/texture.h:9-31).
+ *
+ * Conventions
+ *  - Plain C types only; every pointer is caller-owned unless stated.
+ *  - Errors are returned as are_status codes, never thrown.  are_last_error()
+ *    gives a human-readable message for the calling thread's last failure.
+ *  - A scene handle is immutable after creation and may be rendered from one
+ *    host thread at a time (renders on one handle are serialised by the caller).
+ *  - Primitive ids are global: spheres first, then quads, then triangles, in
+ *    the order of the descriptor's arrays.  Closest-hit ties (equal t) go to
+ *    the lower id, as rt.cpp:209-218 keeps the first triangle on equal t.
+ */
+#ifndef AURORA_GB300_H
+#define AURORA_GB300_H
+
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define ARE_API __declspec(dllexport)
+#else
+#define ARE_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum are_status {
+	ARE_OK = 0,
+	ARE_ERR_INVALID_ARGUMENT = 1, /* malformed descriptor, bad sizes, null pointers */
+	ARE_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+	ARE_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+	ARE_ERR_NO_DEVICE = 4,        /* no usable sm_103 device */
+	ARE_ERR_KERNEL_TIMEOUT = 5,   /* a bounded device-side wait gave up */
+	ARE_ERR_INTERNAL = 6          /* device error word set (queue overflow, bad index) */
+} are_status;
+
+/* ---- scene description (flat arrays, copied by are_scene_create) -------- */
+
+enum { ARE_MAT_LAMBERTIAN = 0, ARE_MAT_METAL = 1, ARE_MAT_DIELECTRIC = 2, ARE_MAT_DIFFUSE_LIGHT = 3 };
+enum { ARE_TEX_SOLID = 0, ARE_TEX_CHECKER = 1, ARE_TEX_IMAGE = 2 };
+enum { ARE_MAP_SURFACE_UV = 0, ARE_MAP_SPHERICAL = 1 };
+enum { ARE_BG_CONSTANT = 0, ARE_BG_SKY_GRADIENT = 1 };
+enum { ARE_TRI_REFERENCE_MT = 0, ARE_TRI_WATERTIGHT = 1 };
+
+/* 48 bytes.  Material kinds follow rt.cpp's MaterialType (rt.cpp:104-107:
+ * MAT_DIFFUSE -> LAMBERTIAN, MAT_METAL -> METAL) and the library's
+ * Diffuse / Reflective (src/material/diffuse.cpp, src/material/reflective.cpp);
+ * DIELECTRIC and DIFFUSE_LIGHT have no counterpart in the reference. */
+typedef struct are_material {
+	int32_t type;            /* ARE_MAT_* */
+	int32_t texture;         /* index into textures (albedo); -1 = none (black) */
+	float fuzz;              /* METAL: radius of the random perturbation, [0,1] */
+	float ior;               /* DIELECTRIC: index of refraction */
+	float emit[3];           /* DIFFUSE_LIGHT: radiance emitted from the front face */
+	float reflect_ratio;     /* legacy estimator: rt.cpp Tri::reflect_ratio */
+	float tint[3];           /* legacy estimator: rt.cpp Tri::metal_tint */
+	float pad_;
+} are_material;
+
+/* 64 bytes.  SOLID and CHECKER follow rt.cpp:85-102; IMAGE samples an
+ * RGB texel grid addressed [y][x] like are::Texture::pixel (src/texture.cpp:77-83). */
+typedef struct are_texture {
+	int32_t type;            /* ARE_TEX_* */
+	int32_t mapping;         /* ARE_MAP_* : where (u,v) comes from */
+	float scale;             /* CHECKER: cells per unit of u and v */
+	int32_t width, height;   /* IMAGE: texel grid size */
+	int32_t texel_offset;    /* IMAGE: first texel (RGB float triple) in texels[] */
+	float a[3];              /* SOLID colour / CHECKER even cells */
+	float b[3];              /* CHECKER odd cells */
+	float center[3];         /* SPHERICAL mapping: centre of the sphere */
+	float pad_;
+} are_texture;
+
+typedef struct are_scene_desc {
+	int32_t n_spheres;
+	const float *spheres;       /* n_spheres x 4: centre xyz, radius */
+	const int32_t *sphere_mat;  /* n_spheres material indices */
+	int32_t n_quads;
+	const float *quads;         /* n_quads x 9: corner Q, edge u, edge v */
+	const int32_t *quad_mat;
+	int32_t n_triangles;
+	const float *triangles;     /* n_triangles x 9: v0, v1, v2 */
+	const float *triangle_uv;   /* n_triangles x 6 per-vertex (u,v), or NULL */
+	const int32_t *triangle_mat;
+	int32_t n_materials;
+	const are_material *materials;
+	int32_t n_textures;
+	const are_texture *textures;
+	int64_t n_texels;
+	const float *texels;        /* n_texels x 3 RGB, linear [0,1] */
+	int32_t background;         /* ARE_BG_* */
+	float bg_a[3];              /* constant colour, or gradient bottom (d.y=-1) */
+	float bg_b[3];              /* gradient top (d.y=+1) */
+	int32_t triangle_test;      /* ARE_TRI_* */
+	int32_t bvh_leaf_size;      /* max primitives per BVH leaf; 0 = default (4) */
+} are_scene_desc;
+
+typedef struct are_scene are_scene; /* opaque: device-resident SoA + BVH */
+
+/* ---- camera and render parameters -------------------------------------- */
+
+/* The reference camera is (camPos, camTarget, camUp, fov) with fov the
+ * vertical field of view in degrees (rt.cpp:337-343).  aperture/focus_dist add
+ * a thin lens; aperture 0 is the reference's pinhole exactly. */
+typedef struct are_camera {
+	float lookfrom[3];
+	float lookat[3];
+	float vup[3];
+	float vfov_deg;
+	float aperture;
+	float focus_dist;
+} are_camera;
+
+enum { ARE_EST_PATH = 0, ARE_EST_LEGACY_RT = 1, ARE_EST_GUIDED = 2 };
+enum {
+	ARE_FLAG_DEVICE_OUTPUT = 1,   /* rgb_out / var_out are device pointers */
+	ARE_FLAG_NO_JITTER = 2,       /* sample pixel centres (rt.cpp:364-365) */
+	ARE_FLAG_CLAMP_OUTPUT = 4     /* clamp each pixel to [0,1] (rt.cpp:368) */
+};
+
+typedef struct are_render_params {
+	int32_t width, height;
+	int32_t spp;                /* samples (camera paths) per pixel */
+	int32_t max_depth;          /* segments per path, >= 1 */
+	uint64_t seed;
+	int32_t rr_depth;           /* Russian roulette from this depth on; <0 = off */
+	float t_min;                /* hits must have t > t_min */
+	int32_t estimator;          /* ARE_EST_* */
+	int32_t flags;              /* ARE_FLAG_* */
+	int32_t pool_size;          /* paths in flight; 0 = auto */
+	int32_t chunk;              /* samples per work item; 0 = auto */
+	int32_t block_size;         /* threads per block; 0 = auto */
+	int32_t reserved_;
+} are_render_params;
+
+enum { ARE_KERNEL_INTERSECT = 0, ARE_KERNEL_SHADE = 1, ARE_KERNEL_GENERATE = 2, ARE_KERNEL_OTHER = 3 };
+
+typedef struct are_render_stats {
+	int64_t samples;            /* camera paths completed */
+	int64_t segments;           /* extension rays traced (closest-hit queries) */
+	int64_t iterations;         /* wavefront iterations executed */
+	double device_ms;           /* CUDA-event time of the whole render on its stream */
+	double kernel_ms[4];        /* CUDA-event time per kernel kind (ARE_KERNEL_*) */
+	int64_t kernel_launches[4]; /* launches per kernel kind */
+	int32_t error_word;         /* device error bits, 0 = clean */
+	int32_t reserved_;
+} are_render_stats;
+
+/* ---- entry points ------------------------------------------------------- */
+
+ARE_API const char *are_status_string(are_status s);
+/* Message of the calling thread's most recent failure ("" if none). */
+ARE_API const char *are_last_error(void);
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+ARE_API int32_t are_version(void);
+/* Number of CUDA devices visible (0 when no GPU; never fails). */
+ARE_API int32_t are_device_count(void);
+
+/* Replaces building rt.cpp's Scene (rt.cpp:146-186) / filling an
+ * are::ObjectSet: validates the descriptor, builds the SAH BVH on the host,
+ * and uploads SoA primitive records, BVH nodes, materials and textures to
+ * the current CUDA device.  The descriptor's arrays are copied. */
+ARE_API are_status are_scene_create(const are_scene_desc *desc, are_scene **out);
+ARE_API are_status are_scene_destroy(are_scene *scene);
+/* Host-side BVH statistics of a created scene (no device work). */
+ARE_API are_status are_scene_info(const are_scene *scene, int64_t *n_prims, int64_t *n_nodes,
+	int32_t *max_leaf, int32_t *depth);
+
+/* Replaces rt.cpp:337-374 render(): renders width x height pixels, spp
+ * samples each, writing the mean linear radiance to rgb_out (row-major from
+ * the top row, 3 floats per pixel).  var_out, if not NULL, receives the
+ * per-pixel sample variance of the mean (3 floats per pixel).  Both are host
+ * pointers unless params->flags has ARE_FLAG_DEVICE_OUTPUT.  stats may be NULL. */
+ARE_API are_status are_render(are_scene *scene, const are_camera *camera, const are_render_params *params,
+	float *rgb_out, float *var_out, are_render_stats *stats);
+
+/* Replaces rt.cpp:209-218 intersect() for a batch: closest hit of each ray.
+ * rays: n x 8 floats (origin xyz, t_min, direction xyz, t_max).
+ * hits: n x 4 (t, prim id as int32 bits, u, v); prim id -1 and t = +inf on a miss.
+ * For triangles (u,v) are the barycentrics of v1 and v2 (rt.cpp:123-138);
+ * for quads the planar coordinates along edges u and v; for spheres 0.
+ * device_ptrs != 0 means rays/hits are device pointers.  ms_out may be NULL;
+ * it receives the kernel's CUDA-event time. */
+ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n, float *hits,
+	int32_t device_ptrs, float *ms_out);
+
+/* ---- synthetic workloads ------------------------------------------------ */
+
+enum {
+	ARE_CONFIG_RANDOM_SPHERES = 0,  /* 488 spheres, 400x225, 32 spp, depth 50 */
+	ARE_CONFIG_CORNELL = 1,         /* 19 quads, 600x600, 1024 spp, depth 50 */
+	ARE_CONFIG_MESH = 2,            /* displaced icosphere, 1920x1080, 256 spp, depth 16 */
+	ARE_CONFIG_CORNELL_OCCLUDED = 4,/* Cornell + occluder under the light, depth 16 */
+	ARE_CONFIG_LEGACY_RT = 5        /* rt.cpp's own 34-triangle scene (rt.cpp:153-167) */
+};
+
+typedef struct are_config are_config; /* owns the arrays its descriptor points at */
+
+/* Builds one of the seeded synthetic scenes.  mesh_frequency only affects
+ * ARE_CONFIG_MESH (geodesic frequency n gives 20 n^2 triangles; 0 = 316). */
+ARE_API are_status are_config_build(int32_t config, uint64_t seed, int32_t mesh_frequency, are_config **out);
+ARE_API const are_scene_desc *are_config_desc(const are_config *cfg);
+ARE_API are_status are_config_defaults(const are_config *cfg, are_camera *camera, are_render_params *params);
+ARE_API void are_config_free(are_config *cfg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AURORA_GB300_H */

@@ -1,0 +1,102 @@
+"""Image parity on the GPU: the wavefront path tracer (are_render) against
+the oracle's CPU render of the same estimator.
+
+* same seed: both sides consume the same random numbers, so the images agree
+  to float rounding except where an ulp-level difference in a transcendental
+  sends one path elsewhere; checked with a per-pixel 3-sigma bound and a
+  bound on the fraction of pixels that differ at all;
+* independent seeds: per-pixel 3-sigma test whose failure fraction must stay
+  within a binomial bound around the 0.27 % expected under the null.
+"""
+import numpy as np
+import pytest
+
+from common import are
+
+pytestmark = pytest.mark.gpu
+
+
+def small(cfg, w, h, spp, **kw):
+    s, cam, par = are.build_config(cfg)
+    par = dict(par, width=w, height=h, spp=spp, **kw)
+    return s, cam, par
+
+
+def sigma_test(m1, v1, m2, v2):
+    """Fraction of pixel channels outside 3 sigma; zero-variance channels must
+    match to 1e-5 relative."""
+    sd = np.sqrt(v1 + v2)
+    z = np.abs(m1 - m2)
+    flat = sd == 0
+    bad_flat = flat & (z > 1e-5 * np.maximum(1.0, np.abs(m1)))
+    out = ~flat & (z > 3 * sd)
+    return (out.sum() + bad_flat.sum()) / m1.size, bad_flat.sum()
+
+
+def binomial_bound(n, p=0.0027, k=5.0):
+    return p + k * np.sqrt(p * (1 - p) / n)
+
+
+@pytest.mark.parametrize("cfg,w,h,spp", [(are.CONFIG_CORNELL, 96, 96, 64), (are.CONFIG_RANDOM_SPHERES, 160, 90, 32),
+                                         (are.CONFIG_CORNELL_OCCLUDED, 64, 64, 32)])
+def test_same_seed_matches_oracle(gpu_lib, oracle, nthreads, cfg, w, h, spp):
+    s, cam, par = small(cfg, w, h, spp)
+    m_gpu, v_gpu, st = are.Scene(s).render(cam, par)
+    m_cpu, v_cpu, st_cpu = oracle.render(oracle.prepare(s), cam, par, nthreads=nthreads)
+    assert st["samples"] == w * h * spp == st_cpu["samples"]
+    assert np.isfinite(m_gpu).all() and np.isfinite(v_gpu).all()
+    frac, flat = sigma_test(m_gpu, v_gpu, m_cpu, v_cpu)
+    assert frac <= binomial_bound(m_gpu.size), frac
+    close = np.abs(m_gpu - m_cpu) <= 1e-4 * np.maximum(1e-3, np.abs(m_cpu))
+    assert close.mean() > 0.9, close.mean()
+    # path lengths agree (same random numbers)
+    assert abs(st["segments"] - st_cpu["segments"]) <= 0.01 * st_cpu["segments"]
+
+
+@pytest.mark.parametrize("cfg,w,h,spp", [(are.CONFIG_RANDOM_SPHERES, 100, 56, 256), (are.CONFIG_CORNELL, 48, 48, 1024)])
+def test_independent_seeds_three_sigma(gpu_lib, oracle, nthreads, cfg, w, h, spp):
+    s, cam, par = small(cfg, w, h, spp)
+    m_gpu, v_gpu, _ = are.Scene(s).render(cam, dict(par, seed=11))
+    m_cpu, v_cpu, _ = oracle.render(oracle.prepare(s), cam, dict(par, seed=12), nthreads=nthreads)
+    frac, _ = sigma_test(m_gpu, v_gpu, m_cpu, v_cpu)
+    assert frac <= binomial_bound(m_gpu.size, k=8.0), frac
+
+
+def test_deterministic_across_pool_sizes(gpu_lib):
+    """The image is a pure function of (scene, camera, params, seed): pool
+    size and scheduling do not change a single bit."""
+    s, cam, par = small(are.CONFIG_CORNELL, 80, 80, 32, chunk=8)
+    sc = are.Scene(s)
+    a, va, sa = sc.render(cam, dict(par, pool_size=4096))
+    b, vb, sb = sc.render(cam, dict(par, pool_size=65536))
+    c, vc, _ = sc.render(cam, dict(par, pool_size=65536))
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(b.view(np.uint32), c.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["samples"] == sb["samples"] == 80 * 80 * 32 and sa["error_word"] == 0
+
+
+def test_full_size_cornell_properties(gpu_lib):
+    """BASELINE-size Cornell frame at reduced spp: every sample completes,
+    the image is finite and non-negative, and the mean radiance matches a
+    second render with another seed within its standard error."""
+    s, cam, par = are.build_config(are.CONFIG_CORNELL)
+    par = dict(par, spp=16)
+    sc = are.Scene(s)
+    m1, v1, st1 = sc.render(cam, dict(par, seed=1))
+    m2, v2, st2 = sc.render(cam, dict(par, seed=2))
+    assert st1["samples"] == 600 * 600 * 16 and st1["error_word"] == 0
+    assert np.isfinite(m1).all() and (m1 >= 0).all()
+    se = np.sqrt(v1.sum() + v2.sum()) / m1.size
+    assert abs(m1.mean() - m2.mean()) < 6 * se + 1e-6
+
+
+def test_render_argument_errors(gpu_lib):
+    s, cam, par = small(are.CONFIG_CORNELL, 8, 8, 1)
+    sc = are.Scene(s)
+    for bad in (dict(width=0), dict(spp=0), dict(max_depth=0), dict(max_depth=1000), dict(t_min=-1.0)):
+        with pytest.raises(are.AreError) as e:
+            sc.render(cam, dict(par, **bad))
+        assert e.value.status == 1
+    with pytest.raises(are.AreError):
+        sc.render(dict(cam, vfov_deg=0.0), par)
