@@ -29,7 +29,7 @@ MAP_SURFACE_UV, MAP_SPHERICAL = 0, 1
 BG_CONSTANT, BG_SKY_GRADIENT = 0, 1
 TRI_REFERENCE_MT, TRI_WATERTIGHT = 0, 1
 EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
-FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT = 1, 2, 4
+FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("texture", "<i4"), ("fuzz", "<f4"), ("ior", "<f4"),

@@ -277,7 +277,9 @@ __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 			}
 		}
 	}
-	if (done) atomicAdd(&W.stat[1], done);
+	// one atomic per warp: every lane of the block reaches this point
+	for (int o = 16; o > 0; o >>= 1) done += __shfl_down_sync(0xffffffffu, done, o);
+	if (lane_id() == 0 && done) atomicAdd(&W.stat[1], done);
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
@@ -365,10 +367,11 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	if (p.width <= 0 || p.height <= 0 || p.spp <= 0 || p.max_depth <= 0 || p.max_depth > 255)
 		return bad("width, height, spp must be > 0 and max_depth in [1, 255]");
 	if ((int64_t)p.width * p.height > (1 << 26)) return bad("image too large (max 2^26 pixels)");
-	if (p.estimator != ARE_EST_PATH) return bad("estimator not supported by this entry point");
 	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");
 	if (!(p.t_min >= 0.0f) || !std::isfinite(p.t_min)) return bad("t_min must be finite and >= 0");
 	cudaSetDevice(sc->device);
+	if (p.estimator == ARE_EST_LEGACY_RT) return render_legacy(sc, cam, p, rgb, stats);
+	if (p.estimator != ARE_EST_PATH) return bad("unknown estimator");
 
 	Wave W{};
 	W.npix = p.width * p.height;
@@ -469,13 +472,14 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	if (!st) {
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
 			int par = it & 1;
-			cudaEventRecord(kev[4 * it + 0], s);
+			// external event nodes: the events are recorded each time the graph runs
+			cudaEventRecordWithFlags(kev[4 * it + 0], s, cudaEventRecordExternal);
 			k_intersect<<<g_int, BLOCK, 0, s>>>(S, W, par);
-			cudaEventRecord(kev[4 * it + 1], s);
+			cudaEventRecordWithFlags(kev[4 * it + 1], s, cudaEventRecordExternal);
 			k_shade<<<g_sh, BLOCK, 0, s>>>(S, W, par);
-			cudaEventRecord(kev[4 * it + 2], s);
+			cudaEventRecordWithFlags(kev[4 * it + 2], s, cudaEventRecordExternal);
 			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
-			cudaEventRecord(kev[4 * it + 3], s);
+			cudaEventRecordWithFlags(kev[4 * it + 3], s, cudaEventRecordExternal);
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
 	}
@@ -494,8 +498,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
 			for (int k = 0; k < 3; ++k) {
 				float ms = 0.f;
-				cudaEventElapsedTime(&ms, kev[4 * it + k], kev[4 * it + k + 1]);
-				kms[k] += ms;
+				if (cudaEventElapsedTime(&ms, kev[4 * it + k], kev[4 * it + k + 1]) == cudaSuccess) kms[k] += ms;
 				++launches[k];
 			}
 		}
@@ -505,6 +508,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			st = ARE_ERR_INTERNAL;
 		}
 	}
+	cudaGetLastError();
 	if (!st) {
 		k_resolve<<<std::max(1, std::min(4096, (W.npix + BLOCK - 1) / BLOCK)), BLOCK, 0, s>>>(
 			W, dev_out ? rgb : d_rgb, var ? (dev_out ? var : d_var) : nullptr, (p.flags & ARE_FLAG_CLAMP_OUTPUT) != 0);

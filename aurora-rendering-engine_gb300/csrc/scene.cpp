@@ -227,6 +227,7 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	for (int k = 0; k < 3; ++k) S.bg_a[k] = d->bg_a[k], S.bg_b[k] = d->bg_b[k];
 	S.box_pad = bvh.box_pad;
 	sc->n_prims = n;
+	sc->n_spheres = ns, sc->n_quads = nq, sc->n_triangles = nt;
 	sc->n_nodes = bvh.n_nodes;
 	sc->max_leaf = bvh.max_leaf;
 	sc->depth = bvh.depth;

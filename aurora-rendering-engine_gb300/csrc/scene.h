@@ -15,6 +15,7 @@ struct are_scene {
 	int device = 0;
 	int n_sms = 0;
 	int64_t n_prims = 0, n_nodes = 0;
+	int32_t n_spheres = 0, n_quads = 0, n_triangles = 0;
 	int32_t max_leaf = 0, depth = 0;
 	std::vector<void *> allocations;  // device buffers owned by the scene
 	cudaStream_t stream = nullptr;
@@ -40,6 +41,8 @@ are_status cuda_status(cudaError_t e, const char *what);
 
 are_status scene_create(const are_scene_desc *desc, are_scene **out);
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
+	are_render_stats *stats);
+are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_params &p, float *rgb,
 	are_render_stats *stats);
 are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms);
 

@@ -132,7 +132,9 @@ enum { ARE_EST_PATH = 0, ARE_EST_LEGACY_RT = 1, ARE_EST_GUIDED = 2 };
 enum {
 	ARE_FLAG_DEVICE_OUTPUT = 1,   /* rgb_out / var_out are device pointers */
 	ARE_FLAG_NO_JITTER = 2,       /* sample pixel centres (rt.cpp:364-365) */
-	ARE_FLAG_CLAMP_OUTPUT = 4     /* clamp each pixel to [0,1] (rt.cpp:368) */
+	ARE_FLAG_CLAMP_OUTPUT = 4,    /* clamp each pixel to [0,1] (rt.cpp:368) */
+	ARE_FLAG_LEGACY_MT19937 = 8   /* ARE_EST_LEGACY_RT with rt.cpp's per-row std::mt19937 stream
+	                                 seeded (uint32)seed + y (rt.cpp:348-351): one thread per row */
 };
 
 typedef struct are_render_params {

@@ -137,6 +137,14 @@ void orc_reflect_f64(const double *v, const double *n, double *out);
 void orc_refract_f64(const double *uv, const double *n, double eta, double *out);
 void orc_ppm_quantize(const float *rgb, int64_t n, float gamma, uint8_t *out); /* rt.cpp:384-386 */
 
+/* The reference's own estimator, rt.cpp trace()/computeAO() (rt.cpp:221-374).
+ * rng_mode 1: rt.cpp's per-row std::mt19937 seeded mt_seed + y; rng_mode 0:
+ * counter-based per pixel keyed by p->seed.  rgb: width*height*3. */
+int32_t orc_render_legacy(const orc_ctx *ctx, const orc_camera *cam, const orc_params *p, float *rgb, int32_t rng_mode,
+	uint32_t mt_seed, int32_t nthreads);
+/* std::mt19937(seed): n raw outputs and n uniform_real_distribution<float>(0,1) draws */
+void orc_mt19937(uint32_t seed, int64_t n, uint32_t *out, float *canon);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,7 +93,7 @@ def _scene_struct(s) -> tuple[OrcScene, list]:
     st.materials = mats.ctypes.data if len(mats) else None
     st.n_textures = len(texs)
     st.textures = texs.ctypes.data if len(texs) else None
-    st.n_texels = 0 if tx is None else len(tx)
+    st.n_texels = 0 if tx is None else tx.size // 3
     st.texels = _ptr(tx, _f) if tx is not None else C.cast(None, _f)
     st.background = int(s.background)
     st.bg_a = (C.c_float * 3)(*[float(v) for v in s.bg_a])
@@ -149,6 +149,9 @@ class Oracle:
         L.orc_reflect_f64.argtypes = [_d, _d, _d]
         L.orc_refract_f64.argtypes = [_d, _d, C.c_double, _d]
         L.orc_ppm_quantize.argtypes = [_f, C.c_int64, C.c_float, C.POINTER(C.c_uint8)]
+        L.orc_render_legacy.argtypes = [C.c_void_p, C.POINTER(OrcCamera), C.POINTER(OrcParams), _f, C.c_int32,
+                                        C.c_uint32, C.c_int32]
+        L.orc_mt19937.argtypes = [C.c_uint32, C.c_int64, C.POINTER(C.c_uint32), _f]
         self.lib = L
 
     class Ctx:
@@ -189,6 +192,16 @@ class Oracle:
         assert rc == 0
         shape = (params["height"], params["width"], 3)
         return mean.reshape(shape), var.reshape(shape), {"samples": st.samples, "segments": st.segments}
+
+
+def render_legacy(orc: "Oracle", ctx, cam: dict, params: dict, rng_mode: int, mt_seed: int = 0,
+                  nthreads: int = 8) -> np.ndarray:
+    """rt.cpp's estimator (AO + depth-0 mirror + diffuse paths) on the oracle."""
+    p = params_struct(params)
+    c = camera_struct(cam)
+    out = np.zeros(params["width"] * params["height"] * 3, np.float32)
+    assert orc.lib.orc_render_legacy(ctx.h, C.byref(c), C.byref(p), _ptr(out, _f), rng_mode, mt_seed, nthreads) == 0
+    return out.reshape(params["height"], params["width"], 3)
 
 
 class RefRT:
