@@ -29,34 +29,9 @@
 #include "scene.h"
 #include "shade.cuh"
 #include "traverse.cuh"
+#include "wave.cuh"
 
 namespace are_core {
-
-constexpr int GRAPH_ITERS = 16;  // iterations per graph launch (even)
-constexpr int BLOCK = 256;
-
-struct Wave {
-	// queues: ray records are (o.xyz, slot bits) and (d.xyz, 0)
-	float4 *qo[2], *qd[2];
-	float4 *hit;      // (t, leaf bits, u, v)
-	float4 *st0;      // (beta.xyz, depth | j << 8)
-	float4 *st1;      // (L.xyz, item bits)
-	float4 *acc_s;    // Kahan sum (xyz) per slot
-	float4 *acc_c;    // Kahan compensation per slot
-	float4 *acc_q;    // sum of squares per slot
-	int32_t *term;    // terminated slots
-	unsigned *cnt;    // [0],[1] queue sizes, [2] terminated, [3] next work item, [4] error word
-	unsigned long long *stat;  // [0] segments, [1] samples
-	float4 *item_s;   // per work item: sum (xyz)
-	float4 *item_q;   // per work item: sum of squares
-	int32_t P;
-	int32_t npix, spp, chunk, nchunk;
-	int64_t n_items;
-	int32_t max_depth, rr_depth;
-	float t_min;
-	uint64_t seed;
-	CameraFrame cam;
-};
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -328,6 +303,15 @@ int grid_for(const void *kernel, int n_sms, size_t smem = 0) {
 	return std::max(1, per_sm) * n_sms;
 }
 
+template <class T>
+T *carve(char *&p, size_t count) {
+	T *r = (T *)p;
+	p += (count * sizeof(T) + 255) & ~(size_t)255;
+	return r;
+}
+
+}  // namespace
+
 void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) {
 	// rt.cpp:339-343: forward, right = forward x up, up' = right x forward
 	float fw[3] = { c.lookat[0] - c.lookfrom[0], c.lookat[1] - c.lookfrom[1], c.lookat[2] - c.lookfrom[2] };
@@ -350,15 +334,6 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) 
 	f.width = w;
 	f.height = h;
 }
-
-template <class T>
-T *carve(char *&p, size_t count) {
-	T *r = (T *)p;
-	p += (count * sizeof(T) + 255) & ~(size_t)255;
-	return r;
-}
-
-}  // namespace
 
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *prm, float *rgb, float *var,
 	are_render_stats *stats) {

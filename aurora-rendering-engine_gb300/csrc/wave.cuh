@@ -1,0 +1,48 @@
+// wave.cuh — the wavefront's device-side state (one struct passed by value
+// to every kernel) and the kernels' declarations, shared by the render entry
+// points.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "core.h"
+#include "shade.cuh"
+
+namespace are_core {
+
+constexpr int GRAPH_ITERS = 16;  // iterations per graph launch (even)
+constexpr int BLOCK = 256;
+
+struct Wave {
+	// queues: ray records are (o.xyz, slot bits) and (d.xyz, 0)
+	float4 *qo[2], *qd[2];
+	float4 *hit;      // (t, leaf bits, u, v)
+	float4 *st0;      // (beta.xyz, depth | j << 8)
+	float4 *st1;      // (L.xyz, item bits)
+	float4 *acc_s;    // Kahan sum (xyz) per slot
+	float4 *acc_c;    // Kahan compensation per slot
+	float4 *acc_q;    // sum of squares per slot
+	int32_t *term;    // terminated slots
+	unsigned *cnt;    // [0],[1] queue sizes, [2] terminated, [3] next work item, [4] error word
+	unsigned long long *stat;  // [0] segments, [1] samples
+	float4 *item_s;   // per work item: sum (xyz)
+	float4 *item_q;   // per work item: sum of squares
+	int32_t P;
+	int32_t npix, spp, chunk, nchunk;
+	int64_t n_items;
+	int32_t max_depth, rr_depth;
+	float t_min;
+	uint64_t seed;
+	CameraFrame cam;
+};
+
+// rt.cpp:339-343 camera basis (host)
+void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);
+
+__global__ void k_init(Wave W, int n_first);
+__global__ void k_intersect(DevScene S, Wave W, int par);
+__global__ void k_shade(DevScene S, Wave W, int par);
+__global__ void k_generate(Wave W, int par);
+__global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ var, int clamp);
+
+}  // namespace are_core
