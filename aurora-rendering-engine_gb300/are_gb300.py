@@ -289,6 +289,8 @@ def load(path: str | os.PathLike | None = None):
                                  C.POINTER(C.c_int32)]
     L.are_render.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
                              C.POINTER(RenderStats)]
+    L.are_render_noalloc.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams), C.c_void_p, C.c_void_p,
+                                     C.POINTER(RenderStats)]
     L.are_intersect.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_float)]
     L.are_config_build.argtypes = [C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_void_p)]
     L.are_config_desc.restype = C.POINTER(SceneDesc)

@@ -91,6 +91,11 @@ ARE_API are_status are_render(are_scene *scene, const are_camera *camera, const 
 	return guarded([&] { return are_core::render(scene, camera, params, rgb_out, var_out, stats); });
 }
 
+ARE_API are_status are_render_noalloc(are_scene *scene, const are_camera *camera, const are_render_params *params,
+	float *rgb_out, float *var_out, are_render_stats *stats) {
+	return guarded([&] { return are_core::render_noalloc(scene, camera, params, rgb_out, var_out, stats); });
+}
+
 ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n, float *hits, int32_t device_ptrs,
 	float *ms_out) {
 	return guarded([&] { return are_core::intersect(scene, rays, n, hits, device_ptrs, ms_out); });

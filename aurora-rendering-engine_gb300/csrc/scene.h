@@ -42,6 +42,8 @@ are_status cuda_status(cudaError_t e, const char *what);
 are_status scene_create(const are_scene_desc *desc, are_scene **out);
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
 	are_render_stats *stats);
+are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
+	are_render_stats *stats);
 are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_params &p, float *rgb,
 	are_render_stats *stats);
 are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms);

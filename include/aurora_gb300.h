@@ -203,6 +203,38 @@ ARE_API are_status are_render(are_scene *scene, const are_camera *camera, const 
 ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n, float *hits,
 	int32_t device_ptrs, float *ms_out);
 
+/* ---- rendering without allocating -------------------------------------- */
+
+/* No counterpart in the reference: an extra entry point for callers that may
+ * not allocate device memory while they render — for example code recording
+ * its own CUDA stream capture, where cudaMalloc/cudaFree would break the
+ * capture, or a plugin host that gives a plugin a fixed device-memory budget
+ * and forbids allocations of its own.  Such a caller creates the scene first
+ * (are_scene_create allocates) and then calls are_render_noalloc, which
+ * renders the path estimator (ARE_EST_PATH) like are_render but calls no
+ * cudaMalloc, cudaFree or other allocating routine and creates no streams,
+ * events or graphs.
+ *
+ * Its scratch — at most ARE_NOALLOC_MAX_PATHS paths in flight and one work
+ * item per pixel for at most ARE_NOALLOC_MAX_PIXELS pixels — is one static
+ * device array of ARE_NOALLOC_SCRATCH_BYTES in the library, which every GPU
+ * that loads the library holds until the process exits.  Larger images are
+ * rejected with ARE_ERR_INVALID_ARGUMENT.
+ *
+ * rgb_out (required) and var_out (optional) are DEVICE pointers of
+ * width*height*3 floats.  The result equals are_render's with chunk = spp.
+ * The first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.  All calls
+ * share the array and it keeps the last call's contents (each call clears what
+ * must start at zero); calls that overlap on the GPU race on it, so serialise
+ * them.  Statistics report counts; device_ms and kernel_ms stay 0 because no
+ * events are created. */
+#define ARE_NOALLOC_MAX_PATHS 65536
+#define ARE_NOALLOC_MAX_PIXELS 524288
+#define ARE_NOALLOC_SCRATCH_BYTES (28u * 1024u * 1024u)
+ARE_API are_status are_render_noalloc(are_scene *scene, const are_camera *camera, const are_render_params *params,
+	float *rgb_out, float *var_out, are_render_stats *stats);
+
 /* ---- synthetic workloads ------------------------------------------------ */
 
 enum {
