@@ -28,6 +28,10 @@ constexpr float PRIM_TAG_TRI = -2.0f;
 constexpr int MAX_STACK = 64;      // traversal stack entries per ray
 constexpr int MAX_BVH_DEPTH = 60;  // the builder never exceeds this
 constexpr int SMEM_NODES = 1024;   // top BVH nodes staged in shared memory (32 KB)
+// scenes with at most this many primitives are scanned linearly from shared
+// memory (4 float4 per primitive) instead of traversing the BVH
+constexpr int LINEAR_MAX = 48;
+static_assert(4 * LINEAR_MAX <= 2 * SMEM_NODES, "staged primitives must fit the node buffer");
 
 // error bits of the device error word
 enum : uint32_t {

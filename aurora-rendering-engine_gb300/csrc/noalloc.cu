@@ -36,10 +36,10 @@ namespace are_core {
 
 namespace {
 
-constexpr size_t NA_SLOT_BYTES = 9 * sizeof(float4) + sizeof(int32_t);  // 2 queues x 2, hit, state x 2, accum x 3, list
+constexpr size_t NA_SLOT_BYTES = WAVE_SLOT_BYTES;  // queues, hit, finished record, accumulators
 constexpr size_t NA_ITEM_BYTES = 2 * sizeof(float4);                  // per-pixel sum and sum of squares
 constexpr size_t NA_SCRATCH = (size_t)ARE_NOALLOC_MAX_PATHS * NA_SLOT_BYTES + (size_t)ARE_NOALLOC_MAX_PIXELS * NA_ITEM_BYTES +
-	64 * sizeof(unsigned) + 8 * sizeof(unsigned long long) + 15 * 256;  // 15 arrays, each padded to 256 bytes
+	64 * sizeof(unsigned) + 8 * sizeof(unsigned long long) + 18 * 256;  // 18 arrays, each padded to 256 bytes
 static_assert(NA_SCRATCH <= (size_t)ARE_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
 
 }  // namespace
@@ -122,12 +122,13 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	W.seed = p.seed;
 	camera_frame(*cam, p.width, p.height, p.flags, W.cam);
 	unsigned char *z = base;
-	for (int q = 0; q < 2; ++q) W.qo[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.qd[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
+	for (int q = 0; q < 2; ++q)
+		W.qa[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.qb[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS),
+		W.qc[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.qd[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.hit = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
-	W.st0 = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.st1 = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
+	W.ta = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.tb = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.acc_s = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.acc_c = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.acc_q = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
-	W.term = take<int32_t>(z, ARE_NOALLOC_MAX_PATHS);
 	W.item_s = take<float4>(z, ARE_NOALLOC_MAX_PIXELS);
 	W.item_q = take<float4>(z, ARE_NOALLOC_MAX_PIXELS);
 	W.cnt = take<unsigned>(z, 64);

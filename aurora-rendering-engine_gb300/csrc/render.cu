@@ -58,16 +58,22 @@ __device__ __forceinline__ void stage_nodes(const DevScene &S, float4 *snodes, i
 __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const float4 *__restrict__ rays, int64_t n,
 	float4 *__restrict__ hits, unsigned *err_word) {
 	__shared__ float4 snodes[2 * SMEM_NODES];
-	int n_snodes;
-	stage_nodes(S, snodes, n_snodes);
+	int n_snodes = 0;
+	const bool linear = S.n_prims <= LINEAR_MAX;
+	if (linear) {
+		stage_prims(S, snodes);
+		__syncthreads();
+	} else {
+		stage_nodes(S, snodes, n_snodes);
+	}
 	uint32_t err = 0;
 	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
 		Hit h;
-		if (S.n_prims > 0) {
-			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
+		if (linear) {
+			h = closest_hit_linear(snodes, S.n_prims, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w);
 		} else {
-			h.leaf = -1;
+			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
 		}
 		hits[i] = h.leaf >= 0 ? make_float4(h.t, __int_as_float(h.gid), h.u, h.v)
 							  : make_float4(__int_as_float(0x7f800000), __int_as_float(-1), 0.f, 0.f);
@@ -78,15 +84,24 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 // ---------------------------------------------------------------------------
 // wavefront kernels
 
-__device__ __forceinline__ void start_sample(const Wave &W, int slot, int64_t item, int j) {
-	// j-th sample of work item `item` begins in `slot`: state only
-	W.st0[slot] = make_float4(1.f, 1.f, 1.f, __int_as_float(j << 8));
-	W.st1[slot] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)item));
+__device__ __forceinline__ void item_coords(const Wave &W, int64_t item, int j, int &pixel, int &sample) {
+	const uint32_t it = (uint32_t)item, np = (uint32_t)W.npix;  // n_items < 2^32 (checked on the host)
+	const uint32_t chunk = it / np;
+	pixel = (int)(it - chunk * np);
+	sample = (int)chunk * W.chunk + j;
 }
 
-__device__ __forceinline__ void item_coords(const Wave &W, int64_t item, int j, int &pixel, int &sample) {
-	pixel = (int)(item % W.npix);
-	sample = (int)(item / W.npix) * W.chunk + j;
+// queue record of a fresh camera path for (item, j) in `slot`
+__device__ __forceinline__ void put_camera_ray(const Wave &W, int q, unsigned pos, int slot, int64_t item, int j) {
+	int pixel, sample;
+	item_coords(W, item, j, pixel, sample);
+	uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+	f3 o, d;
+	camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
+	W.qa[q][pos] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
+	W.qb[q][pos] = make_float4(d.x, d.y, d.z, __int_as_float(j << 8));
+	W.qc[q][pos] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)item));
+	W.qd[q][pos] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 __global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
@@ -95,35 +110,35 @@ __global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
 		W.acc_s[s] = make_float4(0.f, 0.f, 0.f, 0.f);
 		W.acc_c[s] = make_float4(0.f, 0.f, 0.f, 0.f);
 		W.acc_q[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-		if (s >= n_first) continue;
-		start_sample(W, s, s, 0);
-		int pixel, sample;
-		item_coords(W, s, 0, pixel, sample);
-		uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
-		f3 o, d;
-		camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
-		W.qo[0][s] = make_float4(o.x, o.y, o.z, __int_as_float(s));
-		W.qd[0][s] = make_float4(d.x, d.y, d.z, 0.f);
+		if (s < n_first) put_camera_ray(W, 0, (unsigned)s, s, s, 0);
 	}
 }
 
 __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par) {
 	__shared__ float4 snodes[2 * SMEM_NODES];
-	int n_snodes;
+	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		W.cnt[par ^ 1] = 0;  // output queue of this iteration
-		W.cnt[2] = 0;        // terminated list
+		W.cnt[2] = 0;        // finished list
 		atomicAdd(&W.stat[0], (unsigned long long)n);
 	}
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
-	stage_nodes(S, snodes, n_snodes);
-	const float4 *__restrict__ qo = W.qo[par];
-	const float4 *__restrict__ qd = W.qd[par];
+	const bool linear = S.n_prims <= LINEAR_MAX;
+	if (linear) {
+		stage_prims(S, snodes);
+		__syncthreads();
+	} else {
+		stage_nodes(S, snodes, n_snodes);
+	}
+	const float4 *__restrict__ qa = W.qa[par];
+	const float4 *__restrict__ qb = W.qb[par];
 	uint32_t err = 0;
+	const float inf = __int_as_float(0x7f800000);
 	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float4 r0 = qo[i], r1 = qd[i];
-		Hit h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, __int_as_float(0x7f800000), err);
+		float4 r0 = qa[i], r1 = qb[i];
+		Hit h = linear ? closest_hit_linear(snodes, S.n_prims, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf)
+					   : closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
 		W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}
 	if (err) atomicOr(&W.cnt[4], err);
@@ -131,60 +146,59 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 	const unsigned n = W.cnt[par];
-	const float4 *__restrict__ qo = W.qo[par];
-	const float4 *__restrict__ qd = W.qd[par];
-	float4 *__restrict__ oo = W.qo[par ^ 1];
-	float4 *__restrict__ od = W.qd[par ^ 1];
+	const int out = par ^ 1;
 	uint32_t err = 0;
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		unsigned i = base + threadIdx.x;
 		bool valid = i < n;
 		bool cont = false, term = false;
-		int slot = 0;
-		f3 p, nd;
+		f3 p, nd, beta, L;
+		float4 ra, rb, rc;
 		if (valid) {
-			float4 r0 = qo[i], r1 = qd[i];
+			ra = W.qa[par][i];
+			rb = W.qb[par][i];
+			rc = W.qc[par][i];
+			float4 rd = W.qd[par][i];
 			float4 h = W.hit[i];
-			slot = __float_as_int(r0.w);
-			float4 s0 = W.st0[slot], s1 = W.st1[slot];
-			f3 beta = ld3(s0), L = ld3(s1);
-			int meta = __float_as_int(s0.w);
+			beta = ld3(rc);
+			L = ld3(rd);
+			int meta = __float_as_int(rb.w);
 			int depth = meta & 0xff, j = meta >> 8;
-			int64_t item = (int64_t)(unsigned)__float_as_int(s1.w);
-			f3 o = ld3(r0), d = ld3(r1);
+			f3 o = ld3(ra), d = ld3(rb);
 			int leaf = __float_as_int(h.y);
 			if (leaf < 0) {
 				L = add(L, mulv(beta, background(S, d)));
 			} else {
 				int pixel, sample;
-				item_coords(W, item, j, pixel, sample);
+				item_coords(W, (int64_t)(unsigned)__float_as_int(rc.w), j, pixel, sample);
 				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
 				Surface sf = surface_at(S, leaf, o, d, h.x, h.z, h.w);
 				cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd);
 				if (cont && depth + 1 >= W.max_depth) cont = false;
 				p = sf.p;
-				if (cont) {
-					W.st0[slot] = make_float4(beta.x, beta.y, beta.z, __int_as_float((depth + 1) | (j << 8)));
-				}
 			}
 			term = !cont;
-			W.st1[slot] = make_float4(L.x, L.y, L.z, s1.w);
 		}
-		unsigned pos = warp_append(&W.cnt[par ^ 1], cont);
+		unsigned pos = warp_append(&W.cnt[out], cont);
 		if (cont) {
 			if (pos < (unsigned)W.P) {
-				oo[pos] = make_float4(p.x, p.y, p.z, __int_as_float(slot));
-				od[pos] = make_float4(nd.x, nd.y, nd.z, 0.f);
+				int meta = __float_as_int(rb.w) + 1;  // depth + 1, same sample
+				W.qa[out][pos] = make_float4(p.x, p.y, p.z, ra.w);
+				W.qb[out][pos] = make_float4(nd.x, nd.y, nd.z, __int_as_float(meta));
+				W.qc[out][pos] = make_float4(beta.x, beta.y, beta.z, rc.w);
+				W.qd[out][pos] = make_float4(L.x, L.y, L.z, 0.f);
 			} else {
 				err |= ERR_QUEUE_OVERFLOW;
 			}
 		}
 		unsigned tp = warp_append(&W.cnt[2], term);
 		if (term) {
-			if (tp < (unsigned)W.P)
-				W.term[tp] = slot;
-			else
+			if (tp < (unsigned)W.P) {
+				W.ta[tp] = make_float4(L.x, L.y, L.z, ra.w);
+				W.tb[tp] = make_float4(rc.w, __int_as_float(__float_as_int(rb.w) >> 8), 0.f, 0.f);
+			} else {
 				err |= ERR_QUEUE_OVERFLOW;
+			}
 		}
 	}
 	if (err) atomicOr(&W.cnt[4], err);
@@ -192,22 +206,21 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 
 __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 	const unsigned n = W.cnt[2];
-	float4 *__restrict__ oo = W.qo[par ^ 1];
-	float4 *__restrict__ od = W.qd[par ^ 1];
+	const int out = par ^ 1;
 	uint32_t err = 0;
 	unsigned long long done = 0;
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		unsigned i = base + threadIdx.x;
 		bool valid = i < n;
 		bool emit = false;
-		int slot = 0;
-		f3 o, d;
+		int slot = 0, j = 0;
+		int64_t item = 0;
 		if (valid) {
-			slot = W.term[i];
-			float4 s0 = W.st0[slot], s1 = W.st1[slot];
-			int j = __float_as_int(s0.w) >> 8;
-			int64_t item = (int64_t)(unsigned)__float_as_int(s1.w);
-			f3 L = ld3(s1);
+			float4 a = W.ta[i], b = W.tb[i];
+			slot = __float_as_int(a.w);
+			item = (int64_t)(unsigned)__float_as_int(b.x);
+			j = __float_as_int(b.y);
+			f3 L = ld3(a);
 			if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
 				err |= ERR_NONFINITE;
 				L = f3{ 0.f, 0.f, 0.f };
@@ -221,7 +234,7 @@ __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 			q = make_float4(q.x + L.x * L.x, q.y + L.y * L.y, q.z + L.z * L.z, 0.f);
 			++done;
 			++j;
-			int chunk_len = min(W.chunk, W.spp - (int)(item / W.npix) * W.chunk);
+			int chunk_len = min(W.chunk, W.spp - (int)((uint32_t)item / (uint32_t)W.npix) * W.chunk);
 			if (j >= chunk_len) {
 				// item complete: publish its sums, take the next item
 				W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
@@ -233,23 +246,14 @@ __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 			W.acc_s[slot] = sm;
 			W.acc_c[slot] = cm;
 			W.acc_q[slot] = q;
-			if (item < W.n_items) {
-				start_sample(W, slot, item, j);
-				int pixel, sample;
-				item_coords(W, item, j, pixel, sample);
-				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
-				camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
-				emit = true;
-			}
+			emit = item < W.n_items;
 		}
-		unsigned pos = warp_append(&W.cnt[par ^ 1], emit);
+		unsigned pos = warp_append(&W.cnt[out], emit);
 		if (emit) {
-			if (pos < (unsigned)W.P) {
-				oo[pos] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
-				od[pos] = make_float4(d.x, d.y, d.z, 0.f);
-			} else {
+			if (pos < (unsigned)W.P)
+				put_camera_ray(W, out, pos, slot, item, j);
+			else
 				err |= ERR_QUEUE_OVERFLOW;
-			}
 		}
 	}
 	// one atomic per warp: every lane of the block reaches this point
@@ -355,7 +359,8 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	int P = p.pool_size > 0 ? p.pool_size : (1 << 20);
 	if (P > (1 << 24)) return bad("pool_size too large (max 2^24)");
 	int chunk = p.chunk;
-	if (chunk <= 0) chunk = (int)std::min<int64_t>(64, std::max<int64_t>(1, total / (4 * (int64_t)P)));
+	// small work items keep the end-of-frame tail short (a slot finishes its item before going idle)
+	if (chunk <= 0) chunk = (int)std::min<int64_t>(16, std::max<int64_t>(1, total / (16 * (int64_t)P)));
 	chunk = std::min(chunk, p.spp);
 	W.chunk = chunk;
 	W.nchunk = (p.spp + chunk - 1) / chunk;
@@ -374,11 +379,11 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	size_t need = 0;
 	{
 		char *z = nullptr;
-		for (int q = 0; q < 2; ++q) carve<float4>(z, P), carve<float4>(z, P);
-		carve<float4>(z, P);  // hit
-		carve<float4>(z, P), carve<float4>(z, P);
+		for (int q = 0; q < 2; ++q)
+			carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
+		carve<float4>(z, P);                      // hit
+		carve<float4>(z, P), carve<float4>(z, P);  // finished records
 		carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
-		carve<int32_t>(z, P);
 		carve<unsigned>(z, 64);
 		carve<unsigned long long>(z, 8);
 		need = (size_t)z;
@@ -401,11 +406,12 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	}
 	{
 		char *z = (char *)sc->ws;
-		for (int q = 0; q < 2; ++q) W.qo[q] = carve<float4>(z, P), W.qd[q] = carve<float4>(z, P);
+		for (int q = 0; q < 2; ++q)
+			W.qa[q] = carve<float4>(z, P), W.qb[q] = carve<float4>(z, P), W.qc[q] = carve<float4>(z, P),
+			W.qd[q] = carve<float4>(z, P);
 		W.hit = carve<float4>(z, P);
-		W.st0 = carve<float4>(z, P), W.st1 = carve<float4>(z, P);
+		W.ta = carve<float4>(z, P), W.tb = carve<float4>(z, P);
 		W.acc_s = carve<float4>(z, P), W.acc_c = carve<float4>(z, P), W.acc_q = carve<float4>(z, P);
-		W.term = carve<int32_t>(z, P);
 		W.cnt = carve<unsigned>(z, 64);
 		W.stat = carve<unsigned long long>(z, 8);
 		W.item_s = (float4 *)sc->items;

@@ -71,18 +71,56 @@ __device__ __forceinline__ bool hit_sphere(float4 s0, f3 o, f3 d, float tmin, fl
 
 // Quad (Q, u, v): plane hit (src/basic/plane.cpp:13-27), then the planar
 // coordinates alpha, beta in [0,1]^2.  New primitive.
-__device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmin, float tmax, float &tout,
-	float &uo, float &vo) {
+__device__ __forceinline__ bool quad_t_reject(float num, float denom, float tmin, float tcut);
+
+__device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmin, float tmax, float tcut,
+	float &tout, float &uo, float &vo) {
 	f3 n = rcross(u, v);
 	float denom = rdot(n, d);
 	if (denom == 0.0f) return false;
-	float t = __fdiv_rn(rdot(n, rsub(Q, o)), denom);
+	float num = rdot(n, rsub(Q, o));
+	if (quad_t_reject(num, denom, tmin, tcut)) return false;
+	float t = __fdiv_rn(num, denom);
 	if (!(t > tmin && t < tmax)) return false;
 	f3 p = rsub(radd(o, rscl(d, t)), Q);
 	float nn = rdot(n, n);
 	float al = __fdiv_rn(rdot(n, rcross(p, v)), nn);
 	float be = __fdiv_rn(rdot(n, rcross(u, p)), nn);
 	if (!(al >= 0.0f && al <= 1.0f && be >= 0.0f && be <= 1.0f)) return false;
+	tout = t;
+	uo = al;
+	vo = be;
+	return true;
+}
+
+// Quad with the normal n = u x v and nn = n.n precomputed by the same rounded
+// operations as hit_quad, so the result is bit-identical to hit_quad's.
+//
+// Two early rejections skip the divisions without changing any answer:
+//  * with tmin >= 0, t = num/denom is <= 0 whenever num and denom differ in
+//    sign or num is 0, so such planes are behind the ray;
+//  * with lim = tcut * |denom| * (1 + 2^-19) a normal float, |num| > lim means
+//    the correctly rounded quotient exceeds tcut (the best hit so far), so the
+//    quad cannot win; ties (t == tcut) are never rejected.
+__device__ __forceinline__ bool quad_t_reject(float num, float denom, float tmin, float tcut) {
+	if (tmin >= 0.0f && !((num > 0.0f) == (denom > 0.0f) && num != 0.0f)) return true;
+	float lim = tcut * fabsf(denom) * 1.000002f;
+	return lim >= 1.17549435e-38f && fabsf(num) > lim;
+}
+
+__device__ __forceinline__ bool hit_quad_pre(f3 Q, f3 u, f3 v, f3 n, float nn, f3 o, f3 d, float tmin, float tmax,
+	float tcut, float &tout, float &uo, float &vo) {
+	float denom = rdot(n, d);
+	if (denom == 0.0f) return false;
+	float num = rdot(n, rsub(Q, o));
+	if (quad_t_reject(num, denom, tmin, tcut)) return false;
+	float t = __fdiv_rn(num, denom);
+	if (!(t > tmin && t < tmax)) return false;
+	f3 p = rsub(radd(o, rscl(d, t)), Q);
+	float al = __fdiv_rn(rdot(n, rcross(p, v)), nn);
+	if (!(al >= 0.0f && al <= 1.0f)) return false;
+	float be = __fdiv_rn(rdot(n, rcross(u, p)), nn);
+	if (!(be >= 0.0f && be <= 1.0f)) return false;
 	tout = t;
 	uo = al;
 	vo = be;
@@ -158,6 +196,66 @@ struct Hit {
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
+// Stages the primitives of a scene with at most LINEAR_MAX of them into
+// shared memory: per primitive [0..2] the leaf-order record (global id in
+// [1].w), [3] the quad normal u x v and its squared length.
+__device__ __forceinline__ void stage_prims(const DevScene &S, float4 *sp) {
+	for (int j = threadIdx.x; j < S.n_prims; j += blockDim.x) {
+		const float4 *P = S.prims + 3 * (size_t)j;
+		float4 p0 = __ldg(P), p1 = __ldg(P + 1), p2 = __ldg(P + 2);
+		p1.w = __int_as_float(__ldg(S.prim_gid + j));
+		float4 p3 = make_float4(0.f, 0.f, 0.f, 0.f);
+		if (p0.w == PRIM_TAG_QUAD) {
+			f3 n = rcross(ld3(p1), ld3(p2));
+			p3 = make_float4(n.x, n.y, n.z, rdot(n, n));
+		}
+		sp[4 * j] = p0, sp[4 * j + 1] = p1, sp[4 * j + 2] = p2, sp[4 * j + 3] = p3;
+	}
+}
+
+// Closest hit by a linear scan of the staged primitives: rt.cpp's own
+// strategy (rt.cpp:209-218).  Every lane of a warp walks the same primitive
+// at the same time, so the loads are shared-memory broadcasts and the control
+// flow only diverges inside a primitive test.  Same answer as closest_hit.
+__device__ __forceinline__ Hit closest_hit_linear(const float4 *__restrict__ sp, int n, int tri_wt, f3 o, f3 d,
+	float tmin, float tmax) {
+	Hit best;
+	best.t = __int_as_float(0x7f800000);
+	best.leaf = -1;
+	best.gid = 0x7fffffff;
+	best.u = best.v = 0.0f;
+	for (int j = 0; j < n; ++j) {
+		float4 p0 = sp[4 * j];
+		float t, u = 0.0f, v = 0.0f;
+		bool h;
+		float4 p1 = sp[4 * j + 1];
+		if (p0.w > 0.0f) {
+			h = hit_sphere(p0, o, d, tmin, tmax, t);
+		} else {
+			float4 p2 = sp[4 * j + 2];
+			if (p0.w == PRIM_TAG_QUAD) {
+				float4 p3 = sp[4 * j + 3];
+				h = hit_quad_pre(ld3(p0), ld3(p1), ld3(p2), ld3(p3), p3.w, o, d, tmin, tmax, best.t, t, u, v);
+			} else if (tri_wt) {
+				h = hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+			} else {
+				h = hit_tri_mt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+			}
+		}
+		if (h) {
+			int32_t gid = __float_as_int(p1.w);
+			if (t < best.t || (t == best.t && gid < best.gid)) {
+				best.t = t;
+				best.leaf = j;
+				best.gid = gid;
+				best.u = u;
+				best.v = v;
+			}
+		}
+	}
+	return best;
+}
+
 // Closest hit with the (t, global id) order.  `snodes` holds the first
 // `n_snodes` nodes in shared memory.  err receives ERR_* bits.
 __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
@@ -178,6 +276,7 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 	if (S.n_prims == 0) return best;
 
 	int2 stack[MAX_STACK];
+	float stack_t[MAX_STACK];  // entry distance of each pushed node
 	int sp = 0;
 	// current node (a, b): start with the root's
 	float4 r1 = n_snodes > 0 ? snodes[1] : ldg4(G + 1);
@@ -236,6 +335,7 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 					farn = t;
 				}
 				if (sp < MAX_STACK) {
+					stack_t[sp] = fmaxf(l0, l1);
 					stack[sp++] = farn;
 				} else {
 					err |= ERR_STACK_OVERFLOW;
@@ -266,7 +366,7 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 				} else {
 					float4 p1 = ldg4(P + 1), p2 = ldg4(P + 2);
 					if (p0.w == PRIM_TAG_QUAD)
-						h = hit_quad(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+						h = hit_quad(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, best.t, t, u, v);
 					else if (tri_wt)
 						h = hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
 					else
@@ -284,10 +384,18 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 				}
 			}
 		}
-		if (sp == 0) break;
-		int2 nx = stack[--sp];
-		a = nx.x;
-		b = nx.y;
+		// pop, skipping nodes whose entry lies beyond the best hit found since the push
+		bool found = false;
+		while (sp > 0) {
+			--sp;
+			if (stack_t[sp] <= best.t * 1.0000039f) {
+				a = stack[sp].x;
+				b = stack[sp].y;
+				found = true;
+				break;
+			}
+		}
+		if (!found) break;
 	}
 	return best;
 }

@@ -14,16 +14,18 @@ constexpr int GRAPH_ITERS = 16;  // iterations per graph launch (even)
 constexpr int BLOCK = 256;
 
 struct Wave {
-	// queues: ray records are (o.xyz, slot bits) and (d.xyz, 0)
-	float4 *qo[2], *qd[2];
-	float4 *hit;      // (t, leaf bits, u, v)
-	float4 *st0;      // (beta.xyz, depth | j << 8)
-	float4 *st1;      // (L.xyz, item bits)
+	// Ray queues: one 64-byte record per queued path segment, SoA over 4 float4:
+	//   qa = (origin, slot bits)  qb = (direction, depth | j << 8)
+	//   qc = (throughput, item bits)  qd = (radiance so far, 0)
+	// The path state travels with its ray, so every kernel reads and writes
+	// its records in queue order; only the per-slot accumulators are gathered.
+	float4 *qa[2], *qb[2], *qc[2], *qd[2];
+	float4 *hit;      // (t, leaf bits, u, v) per queue position
+	float4 *ta, *tb;  // finished paths: (radiance, slot bits), (item bits, j bits, 0, 0)
 	float4 *acc_s;    // Kahan sum (xyz) per slot
 	float4 *acc_c;    // Kahan compensation per slot
 	float4 *acc_q;    // sum of squares per slot
-	int32_t *term;    // terminated slots
-	unsigned *cnt;    // [0],[1] queue sizes, [2] terminated, [3] next work item, [4] error word
+	unsigned *cnt;    // [0],[1] queue sizes, [2] finished, [3] next work item, [4] error word
 	unsigned long long *stat;  // [0] segments, [1] samples
 	float4 *item_s;   // per work item: sum (xyz)
 	float4 *item_q;   // per work item: sum of squares
@@ -35,6 +37,9 @@ struct Wave {
 	uint64_t seed;
 	CameraFrame cam;
 };
+
+// bytes of wavefront state per path slot (queues x 2, hit, finished record, accumulators)
+constexpr size_t WAVE_SLOT_BYTES = 2 * 4 * sizeof(float4) + sizeof(float4) + 2 * sizeof(float4) + 3 * sizeof(float4);
 
 // rt.cpp:339-343 camera basis (host)
 void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);

@@ -42,7 +42,13 @@ for _p in (str(REPO), str(PKG)):
 
 METRIC = "Msamples/s on 1 GB300 vs host CPU ref; equal-time relMSE, guided vs plain"
 UNIT = "Msamples/s"
-WORKLOAD = "cornell_box_600x600_1024spp_depth50"
+# name -> (config id, label); the default is the Cornell frame the metric is quoted on
+WORKLOADS = {
+    "cornell": (1, "cornell_box_600x600_1024spp_depth50"),
+    "spheres": (0, "random_spheres_400x225_32spp_depth50"),
+    "mesh": (2, "displaced_icosphere_2M_tris_1920x1080_256spp_depth16"),
+}
+WORKLOAD = WORKLOADS["cornell"][1]
 # algorithmic bytes of the wavefront's compulsory SoA traffic per path segment
 BYTES_INTERSECT = 32 + 16                    # ray record in, hit record out
 BYTES_SHADE = 32 + 16 + 32 + 32 + 32 + 4      # ray, hit, path state read + write, next ray, list index
@@ -173,10 +179,11 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--spp", type=int, default=1024)
+    ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's own)")
     ap.add_argument("--pool", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     rank, world, local = dist_env()
     pg = None
@@ -199,8 +206,10 @@ def main() -> None:
 
     torch.cuda.set_device(local)
     L = are.load()
-    scene_arrays, cam, par = are.build_config(are.CONFIG_CORNELL)
-    par = dict(par, spp=args.spp, pool_size=args.pool, chunk=args.chunk)
+    cfg_id, workload = WORKLOADS[args.workload]
+    scene_arrays, cam, par = are.build_config(cfg_id)
+    spp = args.spp if args.spp > 0 else par["spp"]
+    par = dict(par, spp=spp, pool_size=args.pool, chunk=args.chunk)
     W, H = par["width"], par["height"]
     samples_per_step = W * H * par["spp"]
     sc = are.Scene(scene_arrays)
@@ -288,8 +297,8 @@ def main() -> None:
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
-                       "rr_depth": par["rr_depth"], "scene": "cornell box, 18 quads", "parallelism": f"replicas{world}",
+            "config": {"workload": workload, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
+                       "rr_depth": par["rr_depth"], "primitives": scene_arrays.n_prims, "parallelism": f"replicas{world}",
                        "l2": "flushed (256 MB write) between steps; path pool > L2"},
             "segments_per_sample": round(segments / max(1, samples), 4),
             "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,

@@ -83,6 +83,23 @@ def test_workload_scenes(gpu_lib, oracle, nthreads, cfg, kw):
     assert_bitexact(oracle.intersect(ctx, r, nthreads), h, f"config {cfg}")
 
 
+def test_quads_through_the_bvh(gpu_lib, oracle, nthreads):
+    """Three Cornell boxes side by side: more quads than the linear shared-memory
+    scan takes, so quads go through the BVH."""
+    s, _, _ = are.build_config(are.CONFIG_CORNELL)
+    q = s.quads
+    big = are.SceneArrays(materials=s.materials, textures=s.textures)
+    for k in range(3):
+        qq = q.copy()
+        qq[:, 0] += 600.0 * k
+        big.add_quads(qq, s.quad_mat)
+    assert big.n_prims > 48
+    sc = are.Scene(big)
+    r = random_rays(1_000_000, 8, lo=0, hi=1700, t_min=1e-3, t_max=np.inf, camera=(900, 278, -800))
+    h, _ = sc.intersect(r)
+    assert_bitexact(oracle.intersect(oracle.prepare(big), r, nthreads), h, "quads via BVH")
+
+
 def test_full_mesh_ten_million_rays_sampled(gpu_lib, oracle, nthreads):
     """The 2M-triangle mesh: 10M rays on the GPU, a 200k sample checked
     against the oracle's BVH."""
