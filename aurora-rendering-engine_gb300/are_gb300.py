@@ -31,6 +31,7 @@ TRI_REFERENCE_MT, TRI_WATERTIGHT = 0, 1
 EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
 FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
+CONFIG_SPHERE_FIELD = 6
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("texture", "<i4"), ("fuzz", "<f4"), ("ior", "<f4"),
                            ("emit", "<f4", 3), ("reflect_ratio", "<f4"), ("tint", "<f4", 3), ("pad_", "<f4")])
@@ -177,15 +178,34 @@ class RenderParams(C.Structure):
 KERNELS = ("intersect", "shade", "generate", "other")
 
 
+class BatchOptions(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("fetch", C.c_int32), ("leaf_size", C.c_int32), ("reserved_", C.c_int32)]
+
+    def to_dict(self) -> dict:
+        return {"block_size": self.block_size, "fetch": self.fetch, "leaf_size": self.leaf_size}
+
+
+class GuideParams(C.Structure):
+    _fields_ = [("mix", C.c_float), ("guide_depth", C.c_int32), ("train", C.c_int32), ("batch", C.c_int32),
+                ("lr", C.c_float), ("weight_clip", C.c_float), ("reserved_", C.c_int32 * 2)]
+
+    @staticmethod
+    def make(mix=0.5, guide_depth=2, train=1, batch=1 << 18, lr=1e-2, weight_clip=100.0) -> "GuideParams":
+        g = GuideParams()
+        g.mix, g.guide_depth, g.train, g.batch, g.lr, g.weight_clip = mix, guide_depth, train, batch, lr, weight_clip
+        return g
+
+
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("segments", C.c_int64), ("iterations", C.c_int64),
                 ("device_ms", C.c_double), ("kernel_ms", C.c_double * 4), ("kernel_launches", C.c_int64 * 4),
-                ("error_word", C.c_int32), ("reserved_", C.c_int32)]
+                ("error_word", C.c_int32), ("reserved_", C.c_int32), ("aux", C.c_double * 4)]
 
     def to_dict(self) -> dict:
         d = {k: getattr(self, k) for k in ("samples", "segments", "iterations", "device_ms", "error_word")}
         d["kernel_ms"] = dict(zip(KERNELS, list(self.kernel_ms)))
         d["kernel_launches"] = dict(zip(KERNELS, list(self.kernel_launches)))
+        d["aux"] = list(self.aux)
         return d
 
 
@@ -297,6 +317,23 @@ def load(path: str | os.PathLike | None = None):
     L.are_config_desc.argtypes = [C.c_void_p]
     L.are_config_defaults.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams)]
     L.are_config_free.argtypes = [C.c_void_p]
+    L.are_render_guided.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Camera), C.POINTER(RenderParams),
+                                    C.POINTER(GuideParams), C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]
+    L.are_render_batch.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Camera), C.POINTER(RenderParams), C.c_int32,
+                                   C.POINTER(BatchOptions), C.POINTER(C.c_void_p), C.POINTER(C.c_double),
+                                   C.POINTER(RenderStats)]
+    L.are_batch_autotune.argtypes = [C.POINTER(C.POINTER(SceneDesc)), C.POINTER(Camera), C.POINTER(RenderParams),
+                                     C.c_int32, C.c_int32, C.POINTER(BatchOptions), C.POINTER(C.c_double)]
+    L.are_guide_loss_history.restype = C.c_int32
+    L.are_guide_loss_history.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    L.are_guide_param_count.restype = C.c_int32
+    L.are_guide_create.argtypes = [C.c_uint64, C.POINTER(C.c_void_p)]
+    L.are_guide_destroy.argtypes = [C.c_void_p]
+    L.are_guide_get_params.argtypes = [C.c_void_p, C.c_void_p]
+    L.are_guide_set_params.argtypes = [C.c_void_p, C.c_void_p]
+    L.are_guide_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    L.are_guide_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p]
+    L.are_guide_train.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.POINTER(C.c_float)]
     for name in exported_symbols():
         fn = getattr(L, name)
         if fn.restype is C.c_int:  # are_status returns
@@ -385,6 +422,27 @@ class Scene:
         shape = (p.height, p.width, 3)
         return rgb.reshape(shape), (var.reshape(shape) if var is not None else None), st.to_dict()
 
+    def render_guided(self, guide: "Guide", cam: dict, params: dict, gparams: "GuideParams | None" = None,
+                      with_var: bool = True):
+        """are_render_guided with host buffers -> (rgb, var, stats incl. 'train_steps')."""
+        p = RenderParams.from_dict(params)
+        p.flags = int(p.flags) & ~FLAG_DEVICE_OUTPUT
+        c = Camera.from_dict(cam)
+        g = gparams or GuideParams.make()
+        n = p.width * p.height * 3
+        rgb = np.empty(n, np.float32)
+        var = np.empty(n, np.float32) if with_var else None
+        st = RenderStats()
+        check(self.lib.are_render_guided(self.h, guide.h, C.byref(c), C.byref(p), C.byref(g), rgb.ctypes.data,
+                                         var.ctypes.data if var is not None else None, C.byref(st)))
+        d = st.to_dict()
+        d["train_steps"] = int(st.aux[1])
+        d["train_samples"] = int(st.aux[0])
+        d["guided_vertices"] = int(st.aux[2])
+        d["last_loss"] = st.aux[3]
+        shape = (p.height, p.width, 3)
+        return rgb.reshape(shape), (var.reshape(shape) if var is not None else None), d
+
     def render_device(self, cam: dict, params: dict, rgb_ptr: int, var_ptr: int | None = None) -> dict:
         p = RenderParams.from_dict(params)
         p.flags = int(p.flags) | FLAG_DEVICE_OUTPUT
@@ -392,3 +450,104 @@ class Scene:
         st = RenderStats()
         check(self.lib.are_render(self.h, C.byref(c), C.byref(p), rgb_ptr, var_ptr, C.byref(st)))
         return st.to_dict()
+
+
+class Guide:
+    """The path-guiding network (are_guide_*): FP16 tensor-core MLP, FP32 master weights."""
+
+    def __init__(self, seed: int = 1):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.are_guide_create(seed, C.byref(h)))
+        self.h = h
+        self.n_params = self.lib.are_guide_param_count()
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.are_guide_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, np.float32)
+        check(self.lib.are_guide_get_params(self.h, p.ctypes.data))
+        return p
+
+    @params.setter
+    def params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        check(self.lib.are_guide_set_params(self.h, p.ctypes.data))
+
+    def forward(self, feat: np.ndarray) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, np.float32).reshape(-1, 9)
+        out = np.empty((len(feat), 48), np.float32)
+        check(self.lib.are_guide_forward(self.h, feat.ctypes.data, len(feat), out.ctypes.data))
+        return out
+
+    def gradient(self, samples: np.ndarray):
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_float()
+        check(self.lib.are_guide_gradient(self.h, samples.ctypes.data, len(samples), C.byref(loss), g.ctypes.data))
+        return loss.value, g
+
+    def loss_history(self) -> list:
+        out = np.zeros(4096, np.float32)
+        n = self.lib.are_guide_loss_history(self.h, out.ctypes.data, len(out))
+        return list(out[:n])
+
+    def train(self, samples: np.ndarray, lr: float = 1e-2) -> float:
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
+        loss = C.c_float()
+        check(self.lib.are_guide_train(self.h, samples.ctypes.data, len(samples), lr, C.byref(loss)))
+        return loss.value
+
+
+def render_batch(scenes: list, cams: list, params: list, options: "BatchOptions | None" = None, want_images=True):
+    """are_render_batch: many scenes in one persistent launch.
+    Returns (images or None, per-scene completion ms, stats)."""
+    L = load()
+    n = len(scenes)
+    hs = (C.c_void_p * n)(*[sc.h.value for sc in scenes])
+    cs = (Camera * n)(*[Camera.from_dict(c) for c in cams])
+    ps = (RenderParams * n)(*[RenderParams.from_dict(p) for p in params])
+    imgs = [np.empty(p["width"] * p["height"] * 3, np.float32) for p in params] if want_images else None
+    outs = (C.c_void_p * n)(*[im.ctypes.data for im in imgs]) if want_images else None
+    ms = (C.c_double * n)()
+    st = RenderStats()
+    check(L.are_render_batch(hs, cs, ps, n, C.byref(options) if options else None, outs, ms, C.byref(st)))
+    if imgs is not None:
+        imgs = [im.reshape(p["height"], p["width"], 3) for im, p in zip(imgs, params)]
+    return imgs, list(ms), st.to_dict()
+
+
+def batch_autotune(arrays: list, cams: list, params: list, calib_spp: int = 2):
+    """are_batch_autotune over leaf size x block size x fetch -> (BatchOptions, ms)."""
+    L = load()
+    n = len(arrays)
+    descs = [desc_struct(a) for a in arrays]
+    dp = (C.POINTER(SceneDesc) * n)(*[C.pointer(d) for d, _ in descs])
+    cs = (Camera * n)(*[Camera.from_dict(c) for c in cams])
+    ps = (RenderParams * n)(*[RenderParams.from_dict(p) for p in params])
+    best = BatchOptions()
+    ms = C.c_double()
+    check(L.are_batch_autotune(dp, cs, ps, n, calib_spp, C.byref(best), C.byref(ms)))
+    return best, ms.value
+
+
+def batch_workload(n_scenes: int = 64, seed: int = 2026, min_count: int = 50, max_count: int = 200_000):
+    """The uneven batch: sphere counts log-uniform in [min_count, max_count],
+    resolution and spp drawn per scene by the scene generator."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n_scenes):
+        cnt = int(np.exp(rng.uniform(np.log(min_count), np.log(max_count))))
+        out.append(build_config(CONFIG_SPHERE_FIELD, seed=seed * 1000 + i, mesh_frequency=cnt))
+    return out

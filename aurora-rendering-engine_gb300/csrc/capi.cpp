@@ -96,6 +96,17 @@ ARE_API are_status are_render_noalloc(are_scene *scene, const are_camera *camera
 	return guarded([&] { return are_core::render_noalloc(scene, camera, params, rgb_out, var_out, stats); });
 }
 
+ARE_API are_status are_render_batch(are_scene *const *scenes, const are_camera *cameras,
+	const are_render_params *params, int32_t n, const are_batch_options *options, float *const *rgb_out,
+	double *scene_ms, are_render_stats *stats) {
+	return guarded([&] { return are_core::render_batch(scenes, cameras, params, n, options, rgb_out, scene_ms, stats); });
+}
+
+ARE_API are_status are_batch_autotune(const are_scene_desc *const *descs, const are_camera *cameras,
+	const are_render_params *params, int32_t n, int32_t calib_spp, are_batch_options *best, double *best_ms) {
+	return guarded([&] { return are_core::batch_autotune(descs, cameras, params, n, calib_spp, best, best_ms); });
+}
+
 ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n, float *hits, int32_t device_ptrs,
 	float *ms_out) {
 	return guarded([&] { return are_core::intersect(scene, rays, n, hits, device_ptrs, ms_out); });

@@ -338,6 +338,47 @@ void mesh(are_config &c, uint64_t seed, int freq) {
 	set_params(c.params, 1920, 1080, 256, 16, 1, 1e-4f);
 }
 
+// One scene of the uneven batch: `count` spheres on a jittered square grid
+// sized to the count (side ceil(sqrt(count)) over 22 units, radius 0.4 of a
+// cell), materials drawn as in random_spheres, on the same ground sphere and
+// camera; resolution and samples per pixel drawn from the seed.
+void sphere_field(are_config &c, uint64_t seed, int count) {
+	SplitMix r{ seed * 0x9E3779B97F4A7C15ULL + 17 };
+	c.sphere(0, -1000, 0, 1000, c.lambertian(0.5f, 0.5f, 0.5f));
+	int side = (int)std::ceil(std::sqrt((double)count));
+	double cell = 22.0 / side, rad = 0.4 * cell;
+	int placed = 0;
+	for (int a = 0; a < side && placed < count; ++a)
+		for (int b = 0; b < side && placed < count; ++b, ++placed) {
+			double choose = r.u();
+			double x = -11.0 + (a + 0.2 + 0.6 * r.u()) * cell, z = -11.0 + (b + 0.2 + 0.6 * r.u()) * cell;
+			int m;
+			if (choose < 0.8) {
+				float alb[3];
+				for (int k = 0; k < 3; ++k) alb[k] = (float)r.u();
+				for (int k = 0; k < 3; ++k) alb[k] *= (float)r.u();
+				m = c.lambertian(alb[0], alb[1], alb[2]);
+			} else if (choose < 0.95) {
+				float alb[3];
+				for (int k = 0; k < 3; ++k) alb[k] = (float)r.u(0.5, 1.0);
+				m = c.material(ARE_MAT_METAL, c.texture(ARE_TEX_SOLID, alb), (float)r.u(0.0, 0.5));
+			} else {
+				float w[3] = { 1.f, 1.f, 1.f };
+				m = c.material(ARE_MAT_DIELECTRIC, c.texture(ARE_TEX_SOLID, w), 0.0f, 1.5f);
+			}
+			c.sphere(x, rad, z, rad, m);
+		}
+	c.desc.background = ARE_BG_SKY_GRADIENT;
+	for (int k = 0; k < 3; ++k) c.desc.bg_a[k] = 1.0f;
+	c.desc.bg_b[0] = 0.5f, c.desc.bg_b[1] = 0.7f, c.desc.bg_b[2] = 1.0f;
+	c.desc.triangle_test = ARE_TRI_WATERTIGHT;
+	set_cam(c.cam, 13, 2, 3, 0, 0, 0, 20, 0.1, 10.0);
+	static const int res[3][2] = { { 256, 256 }, { 640, 360 }, { 1280, 720 } };
+	static const int spps[3] = { 16, 64, 256 };
+	int ri = (int)(r.u() * 3.0), si = (int)(r.u() * 3.0);
+	set_params(c.params, res[std::min(ri, 2)][0], res[std::min(ri, 2)][1], spps[std::min(si, 2)], 50, seed, 1e-3f);
+}
+
 // rt.cpp's own scene (experiments/rt.cpp:153-185), as data: five wall quads
 // and two boxes, each quad split into two triangles with the fixed per-vertex
 // uv of pushQuad, every triangle MAT_METAL with reflect_ratio 0.9.
@@ -422,6 +463,13 @@ are_status config_build(int32_t config, uint64_t seed, int32_t freq, are_config 
 			mesh(*c, seed, freq ? freq : 316);
 			break;
 		case ARE_CONFIG_LEGACY_RT: legacy_rt(*c); break;
+		case ARE_CONFIG_SPHERE_FIELD:
+			if (freq < 1 || freq > 4000000) {
+				set_error("sphere count must be in [1, 4000000]");
+				return ARE_ERR_INVALID_ARGUMENT;
+			}
+			sphere_field(*c, seed, freq);
+			break;
 		default: set_error("unknown config " + std::to_string(config)); return ARE_ERR_INVALID_ARGUMENT;
 		}
 	} catch (const std::bad_alloc &) {

@@ -31,7 +31,7 @@ constexpr int SMEM_NODES = 1024;   // top BVH nodes staged in shared memory (32 
 // scenes with at most this many primitives are scanned linearly from shared
 // memory (4 float4 per primitive) instead of traversing the BVH
 constexpr int LINEAR_MAX = 48;
-static_assert(4 * LINEAR_MAX <= 2 * SMEM_NODES, "staged primitives must fit the node buffer");
+static_assert(6 * LINEAR_MAX <= 2 * SMEM_NODES, "staged primitives must fit the node buffer");
 
 // error bits of the device error word
 enum : uint32_t {
@@ -64,6 +64,8 @@ struct DevScene {
 	const int32_t *prim_mat;
 	const float *tri_uv;       // null if the scene has no per-vertex uv
 	const float4 *nodes;
+	const float4 *leaves;      // leaf boxes (node format) when n_prims <= LINEAR_MAX
+	int32_t n_leaves;
 	const DevMaterial *mats;
 	const DevTexture *texs;
 	const float *texels;

@@ -1,0 +1,708 @@
+// guide.cu — training and inference kernels of the path-guiding network, and
+// the are_guide_* entry points.
+//
+//   k_guide_pack    FP32 master parameters -> FP16 weight image (forward rows
+//                   and transposed rows for the backward pass) + FP32 biases
+//   k_guide_infer   fused forward of 16-row tiles on the tensor cores
+//   k_guide_fwdbwd  fused forward + loss gradient + backward per 16-sample
+//                   tile; stores each layer's input and output gradient (FP16)
+//   k_guide_wgrad   weight gradients dW = sum_s delta_s h_s^T on the tensor
+//                   cores, K = samples, split over blocks, FP32 atomics
+//   k_guide_bgrad   bias gradients
+//   k_guide_adam    Adam on the FP32 master weights, skipped on FP16 overflow
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "guide.cuh"
+#include "guide_host.h"
+#include "scene.h"
+
+namespace are_core {
+
+namespace {
+
+constexpr int GT = 256;  // threads per block of the MLP kernels (8 warps)
+
+__global__ void k_guide_pack(const float *__restrict__ P, __half *__restrict__ img, float *__restrict__ bias) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < IMG_ALL + IMG_BIAS; i += gridDim.x * blockDim.x) {
+		if (i >= IMG_ALL) {
+			int b = i - IMG_ALL;
+			int off = b < 64 ? OFF_B1 + b : b < 128 ? OFF_B2 + b - 64 : b < 192 ? OFF_B3 + b - 128 : b < 256 ? OFF_B4 + b - 192 : OFF_B5 + b - 256;
+			bias[b] = (b >= 256 && b - 256 >= 40) ? 0.f : P[off];
+			continue;
+		}
+		float v = 0.f;
+		if (i < IMG_W2) {
+			int r = i / S_ENC, c = i - r * S_ENC;
+			if (c < GN_ENC) v = P[OFF_W1 + r * GN_ENC + c];
+		} else if (i < IMG_FWD) {
+			int L = i < IMG_W3 ? 2 : i < IMG_W4 ? 3 : i < IMG_W5 ? 4 : 5;
+			int base = L == 2 ? IMG_W2 : L == 3 ? IMG_W3 : L == 4 ? IMG_W4 : IMG_W5;
+			int off = L == 2 ? OFF_W2 : L == 3 ? OFF_W3 : L == 4 ? OFF_W4 : OFF_W5;
+			int r = (i - base) / S_H, c = (i - base) - r * S_H;
+			if (c < GN_H && !(L == 5 && r >= 40)) v = P[off + r * GN_H + c];
+		} else if (i < IMG_W5T) {
+			// transposed [in][out] copies of W2..W4
+			int L = i < IMG_W3T ? 2 : i < IMG_W4T ? 3 : 4;
+			int base = L == 2 ? IMG_W2T : L == 3 ? IMG_W3T : IMG_W4T;
+			int off = L == 2 ? OFF_W2 : L == 3 ? OFF_W3 : OFF_W4;
+			int in = (i - base) / S_H, o = (i - base) - in * S_H;
+			if (o < GN_H) v = P[off + o * GN_H + in];
+		} else {
+			int in = (i - IMG_W5T) / S_OUT, o = (i - IMG_W5T) - in * S_OUT;
+			if (o < 40) v = P[OFF_W5 + o * GN_H + in];
+		}
+		img[i] = __float2half_rn(v);
+	}
+}
+
+// Copies `halves` halves and IMG_BIAS floats of the image into shared memory.
+__device__ __forceinline__ void load_image(const __half *img, const float *bias, int halves, __half *s_img,
+	float *s_bias) {
+	const uint4 *src = reinterpret_cast<const uint4 *>(img);
+	uint4 *dst = reinterpret_cast<uint4 *>(s_img);
+	for (int i = threadIdx.x; i < halves / 8; i += blockDim.x) dst[i] = src[i];
+	for (int i = threadIdx.x; i < IMG_BIAS; i += blockDim.x) s_bias[i] = bias[i];
+	__syncthreads();
+}
+
+// Forward of one 16-row tile; x0/x1 are the features of rows g and g+8.
+// Returns the output C fragments and, if keep != null, the A fragments of the
+// four hidden layers' outputs (inputs of layers 2..5).
+__device__ __forceinline__ void tile_forward(const __half *s_img, const float *s_bias, const float *x0, const float *x1,
+	float (*c5)[4], uint32_t (*keep)[4][4], __half *h0_out0, __half *h0_out1) {
+	const int t = threadIdx.x & 3;
+	float c[8][4];
+#pragma unroll
+	for (int nt = 0; nt < 8; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
+	const int g = (threadIdx.x & 31) >> 2;
+	for (int ks = 0; ks < GN_ENC / 16; ++ks) {
+		uint32_t a[4];
+		a[0] = h2u(enc_pair(x0, ks * 8 + t));
+		a[1] = h2u(enc_pair(x1, ks * 8 + t));
+		a[2] = h2u(enc_pair(x0, ks * 8 + 4 + t));
+		a[3] = h2u(enc_pair(x1, ks * 8 + 4 + t));
+		if (h0_out0) {
+			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 2 * t) = a[0];
+			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 2 * t) = a[1];
+			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 8 + 2 * t) = a[2];
+			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 8 + 2 * t) = a[3];
+		}
+#pragma unroll
+		for (int nt = 0; nt < 8; ++nt) {
+			const __half *row = s_img + IMG_W1 + (nt * 8 + g) * S_ENC + ks * 16 + 2 * t;
+			mma16816(c[nt], a, *reinterpret_cast<const uint32_t *>(row), *reinterpret_cast<const uint32_t *>(row + 8));
+		}
+	}
+	uint32_t a[4][4];
+	relu_to_a(c, s_bias + 0, a);
+	if (keep) memcpy(keep[0], a, sizeof a);
+	tile_layer<4, 8>(a, s_img + IMG_W2, S_H, c);
+	relu_to_a(c, s_bias + 64, a);
+	if (keep) memcpy(keep[1], a, sizeof a);
+	tile_layer<4, 8>(a, s_img + IMG_W3, S_H, c);
+	relu_to_a(c, s_bias + 128, a);
+	if (keep) memcpy(keep[2], a, sizeof a);
+	tile_layer<4, 8>(a, s_img + IMG_W4, S_H, c);
+	relu_to_a(c, s_bias + 192, a);
+	if (keep) memcpy(keep[3], a, sizeof a);
+	tile_layer<4, 6>(a, s_img + IMG_W5, S_H, c5);
+#pragma unroll
+	for (int nt = 0; nt < 6; ++nt) {
+		float b0 = s_bias[256 + nt * 8 + 2 * t], b1 = s_bias[256 + nt * 8 + 2 * t + 1];
+		c5[nt][0] += b0, c5[nt][1] += b1, c5[nt][2] += b0, c5[nt][3] += b1;
+	}
+}
+
+__global__ void __launch_bounds__(GT) k_guide_infer(const __half *__restrict__ img, const float *__restrict__ bias,
+	const float *__restrict__ feat, int n, const unsigned *__restrict__ n_dev, float *__restrict__ out) {
+	if (n_dev) n = min(n, (int)*n_dev);
+	extern __shared__ __align__(16) unsigned char smem[];
+	__half *s_img = reinterpret_cast<__half *>(smem);
+	float *s_bias = reinterpret_cast<float *>(smem + IMG_FWD * sizeof(__half));
+	load_image(img, bias, IMG_FWD, s_img, s_bias);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	const int tiles = (n + 15) / 16;
+	for (int tile = blockIdx.x * (GT / 32) + warp; tile < tiles; tile += gridDim.x * (GT / 32)) {
+		int r0 = tile * 16 + g, r1 = r0 + 8;
+		float x0[GN_IN], x1[GN_IN];
+		for (int k = 0; k < GN_IN; ++k) {
+			x0[k] = r0 < n ? feat[(size_t)r0 * GN_IN + k] : 0.f;
+			x1[k] = r1 < n ? feat[(size_t)r1 * GN_IN + k] : 0.f;
+		}
+		float c5[6][4];
+		tile_forward(s_img, s_bias, x0, x1, c5, nullptr, nullptr, nullptr);
+#pragma unroll
+		for (int nt = 0; nt < 6; ++nt) {
+			int col = nt * 8 + 2 * t;
+			if (r0 < n) out[(size_t)r0 * GN_OUT + col] = c5[nt][0], out[(size_t)r0 * GN_OUT + col + 1] = c5[nt][1];
+			if (r1 < n) out[(size_t)r1 * GN_OUT + col] = c5[nt][2], out[(size_t)r1 * GN_OUT + col + 1] = c5[nt][3];
+		}
+	}
+}
+
+// d(-log q)/d(outputs) of one sample (as oracle/orc_guide.c out_grad), times wt.
+__device__ float sample_out_grad(const float *o, f3 w, float wt, float *g) {
+	Mixture m;
+	to_mixture(o, m);
+	float v[GN_LOBES], q = 0.f;
+	for (int l = 0; l < GN_LOBES; ++l) {
+		float c = m.mu[l].x * w.x + m.mu[l].y * w.y + m.mu[l].z * w.z;
+		v[l] = m.norm[l] * expf(m.kappa[l] * (c - 1.f));
+		q += m.pi[l] * v[l];
+	}
+	q = fmaxf(q, 1e-30f);
+	for (int l = 0; l < GN_LOBES; ++l) {
+		float r = m.pi[l] * v[l] / q;
+		float k = m.kappa[l];
+		float c = m.mu[l].x * w.x + m.mu[l].y * w.y + m.mu[l].z * w.z;
+		float dlogv = 1.f / k - 2.f / expm1f(2.f * k) + (c - 1.f);
+		float sig = 1.f / (1.f + expf(-o[5 * l + 3]));
+		g[5 * l + 3] = -r * dlogv * sig * wt;
+		float dmu[3] = { -r * k * w.x, -r * k * w.y, -r * k * w.z };
+		const float *mm = o + 5 * l;
+		float nm = sqrtf(mm[0] * mm[0] + mm[1] * mm[1] + mm[2] * mm[2]);
+		float len = nm + 1e-6f;
+		float mdot = dmu[0] * mm[0] + dmu[1] * mm[1] + dmu[2] * mm[2];
+		for (int j = 0; j < 3; ++j) g[5 * l + j] = (dmu[j] / len - (nm > 0.f ? mm[j] * mdot / (nm * len * len) : 0.f)) * wt;
+		g[5 * l + 4] = (m.pi[l] - r) * wt;
+	}
+	return -wt * logf(q);
+}
+
+// backward of a hidden layer: C = (delta A) (16 x K_out) x W^T-image, masked
+// by the forward activations `h` (A fragments, h > 0), returned as A fragments.
+template <int KSTEPS>
+__device__ __forceinline__ void back_layer(const uint32_t (*da)[4], const __half *WT, int stride, const uint32_t (*h)[4],
+	uint32_t (*out)[4], float scale_clip) {
+	float c[8][4];
+	tile_layer<KSTEPS, 8>(da, WT, stride, c);
+#pragma unroll
+	for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+		for (int hh = 0; hh < 2; ++hh) {
+			int nt = 2 * ks + hh;
+			__half2 hr0 = u2h(h[ks][2 * hh]), hr1 = u2h(h[ks][2 * hh + 1]);
+			float m0 = __low2float(hr0) > 0.f ? 1.f : 0.f, m1 = __high2float(hr0) > 0.f ? 1.f : 0.f;
+			float m2 = __low2float(hr1) > 0.f ? 1.f : 0.f, m3 = __high2float(hr1) > 0.f ? 1.f : 0.f;
+			float v0 = fminf(fmaxf(c[nt][0] * m0, -scale_clip), scale_clip);
+			float v1 = fminf(fmaxf(c[nt][1] * m1, -scale_clip), scale_clip);
+			float v2 = fminf(fmaxf(c[nt][2] * m2, -scale_clip), scale_clip);
+			float v3 = fminf(fmaxf(c[nt][3] * m3, -scale_clip), scale_clip);
+			out[ks][2 * hh] = h2u(__floats2half2_rn(v0, v1));
+			out[ks][2 * hh + 1] = h2u(__floats2half2_rn(v2, v3));
+		}
+	}
+}
+
+// store A fragments of a 16 x 64 tile to rows r0/r1 of a [n][64] half array
+__device__ __forceinline__ void store_a64(const uint32_t (*a)[4], __half *base, int r0, int r1, int n) {
+	const int t = threadIdx.x & 3;
+#pragma unroll
+	for (int ks = 0; ks < 4; ++ks) {
+		if (r0 < n) {
+			*reinterpret_cast<uint32_t *>(base + (size_t)r0 * GN_H + ks * 16 + 2 * t) = a[ks][0];
+			*reinterpret_cast<uint32_t *>(base + (size_t)r0 * GN_H + ks * 16 + 8 + 2 * t) = a[ks][2];
+		}
+		if (r1 < n) {
+			*reinterpret_cast<uint32_t *>(base + (size_t)r1 * GN_H + ks * 16 + 2 * t) = a[ks][1];
+			*reinterpret_cast<uint32_t *>(base + (size_t)r1 * GN_H + ks * 16 + 8 + 2 * t) = a[ks][3];
+		}
+	}
+}
+
+__global__ void __launch_bounds__(GT, 1) k_guide_fwdbwd(const __half *__restrict__ img, const float *__restrict__ bias,
+	const float *__restrict__ samples, int n, float wscale, const float *__restrict__ wscale_dev, float wclip, float lscale,
+	GuideTrainBufs B, float *__restrict__ loss_sum) {
+	if (wscale_dev) wscale = *wscale_dev;
+	extern __shared__ __align__(16) unsigned char smem[];
+	__half *s_img = reinterpret_cast<__half *>(smem);
+	float *s_bias = reinterpret_cast<float *>(smem + IMG_ALL * sizeof(__half));
+	float *s_out = s_bias + IMG_BIAS;  // per warp 16 x 48 FP32 outputs
+	__half *s_d5 = reinterpret_cast<__half *>(s_out + (GT / 32) * 16 * GN_OUT);  // per warp 16 x S_OUT
+	load_image(img, bias, IMG_ALL, s_img, s_bias);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	float *wo = s_out + warp * 16 * GN_OUT;
+	__half *wd = s_d5 + warp * 16 * S_OUT;
+	const float clip = 60000.f;
+	float lacc = 0.f;
+	const int tiles = (n + 15) / 16;
+	for (int tile = blockIdx.x * (GT / 32) + warp; tile < tiles; tile += gridDim.x * (GT / 32)) {
+		int r0 = tile * 16 + g, r1 = r0 + 8;
+		float x0[GN_IN], x1[GN_IN];
+		for (int k = 0; k < GN_IN; ++k) {
+			x0[k] = r0 < n ? samples[(size_t)r0 * 16 + k] : 0.f;
+			x1[k] = r1 < n ? samples[(size_t)r1 * 16 + k] : 0.f;
+		}
+		float c5[6][4];
+		uint32_t hk[4][4][4];
+		tile_forward(s_img, s_bias, x0, x1, c5, hk, B.h0 + (size_t)(r0 < n ? r0 : B.dump_row) * GN_ENC,
+			B.h0 + (size_t)(r1 < n ? r1 : B.dump_row) * GN_ENC);
+		// outputs to shared memory, one row per lane for the loss
+#pragma unroll
+		for (int nt = 0; nt < 6; ++nt) {
+			wo[g * GN_OUT + nt * 8 + 2 * t] = c5[nt][0];
+			wo[g * GN_OUT + nt * 8 + 2 * t + 1] = c5[nt][1];
+			wo[(g + 8) * GN_OUT + nt * 8 + 2 * t] = c5[nt][2];
+			wo[(g + 8) * GN_OUT + nt * 8 + 2 * t + 1] = c5[nt][3];
+		}
+		__syncwarp();
+		if (lane < 16) {
+			int r = tile * 16 + lane;
+			float gr[GN_OUT];
+			for (int j = 0; j < GN_OUT; ++j) gr[j] = 0.f;
+			if (r < n) {
+				const float *s = samples + (size_t)r * 16;
+				float wt = fminf(s[12] * wscale, wclip);
+				lacc += sample_out_grad(wo + lane * GN_OUT, f3{ s[9], s[10], s[11] }, wt, gr);
+			}
+			for (int j = 0; j < GN_OUT; ++j) {
+				float v = fminf(fmaxf(gr[j] * lscale, -clip), clip);
+				wd[lane * S_OUT + j] = __float2half_rn(v);
+				if (r < n) B.d5[(size_t)r * GN_OUT + j] = wd[lane * S_OUT + j];
+			}
+		}
+		__syncwarp();
+		// backward: delta5 (16 x 48) -> delta4 .. delta1
+		uint32_t da5[3][4];
+#pragma unroll
+		for (int ks = 0; ks < 3; ++ks) {
+			da5[ks][0] = *reinterpret_cast<const uint32_t *>(wd + g * S_OUT + ks * 16 + 2 * t);
+			da5[ks][1] = *reinterpret_cast<const uint32_t *>(wd + (g + 8) * S_OUT + ks * 16 + 2 * t);
+			da5[ks][2] = *reinterpret_cast<const uint32_t *>(wd + g * S_OUT + ks * 16 + 8 + 2 * t);
+			da5[ks][3] = *reinterpret_cast<const uint32_t *>(wd + (g + 8) * S_OUT + ks * 16 + 8 + 2 * t);
+		}
+		uint32_t d4[4][4], d3[4][4], d2[4][4], d1[4][4];
+		back_layer<3>(da5, s_img + IMG_W5T, S_OUT, hk[3], d4, clip);
+		back_layer<4>(d4, s_img + IMG_W4T, S_H, hk[2], d3, clip);
+		back_layer<4>(d3, s_img + IMG_W3T, S_H, hk[1], d2, clip);
+		back_layer<4>(d2, s_img + IMG_W2T, S_H, hk[0], d1, clip);
+		store_a64(d4, B.d[3], r0, r1, n);
+		store_a64(d3, B.d[2], r0, r1, n);
+		store_a64(d2, B.d[1], r0, r1, n);
+		store_a64(d1, B.d[0], r0, r1, n);
+		for (int L = 0; L < 4; ++L) store_a64(hk[L], B.h[L], r0, r1, n);
+		__syncwarp();
+	}
+	for (int o = 16; o > 0; o >>= 1) lacc += __shfl_down_sync(0xffffffffu, lacc, o);
+	if (lane == 0) atomicAdd(loss_sum, lacc);
+}
+
+// dW[o][i] += sum over a chunk of samples of delta[s][o] * h[s][i] on the tensor cores.
+__device__ __forceinline__ uint32_t pack2(const __half *p, size_t stride) {
+	__half2 v = __halves2half2(p[0], p[stride]);
+	return h2u(v);
+}
+
+template <int OUT_TILES, int IN_TILES>
+__device__ void wgrad_layer(const __half *__restrict__ D, int dstride, const __half *__restrict__ H, int hstride, int s0,
+	int s1, float *__restrict__ grad, int gstride, int out_limit, unsigned *overflow) {
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	const int ntiles = OUT_TILES * IN_TILES;
+	for (int tile = warp; tile < ntiles; tile += GT / 32) {
+		int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
+		float c[4] = { 0.f, 0.f, 0.f, 0.f };
+		for (int s = s0; s < s1; s += 16) {
+			uint32_t a[4];
+			const __half *dp = D + (size_t)(s + 2 * t) * dstride + ot * 16 + g;
+			a[0] = pack2(dp, dstride);
+			a[1] = pack2(dp + 8, dstride);
+			a[2] = pack2(dp + (size_t)8 * dstride, dstride);
+			a[3] = pack2(dp + (size_t)8 * dstride + 8, dstride);
+			const __half *hp = H + (size_t)(s + 2 * t) * hstride + it * 8 + g;
+			uint32_t b0 = pack2(hp, hstride), b1 = pack2(hp + (size_t)8 * hstride, hstride);
+			mma16816(c, a, b0, b1);
+		}
+		int o0 = ot * 16 + g, i0 = it * 8 + 2 * t;
+		bool bad = !(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]) && isfinite(c[3]));
+		if (bad) atomicOr(overflow, 1u);
+		if (o0 < out_limit) atomicAdd(&grad[o0 * gstride + i0], c[0]), atomicAdd(&grad[o0 * gstride + i0 + 1], c[1]);
+		if (o0 + 8 < out_limit)
+			atomicAdd(&grad[(o0 + 8) * gstride + i0], c[2]), atomicAdd(&grad[(o0 + 8) * gstride + i0 + 1], c[3]);
+	}
+}
+
+constexpr int WG_CHUNK = 512;
+
+__global__ void __launch_bounds__(GT) k_guide_wgrad(GuideTrainBufs B, int n, float *__restrict__ grad, unsigned *overflow) {
+	// samples are padded to a multiple of 16 with zero gradients
+	int s0 = blockIdx.x * WG_CHUNK, s1 = min(s0 + WG_CHUNK, n);
+	if (s0 >= s1) return;
+	wgrad_layer<4, 32>(B.d[0], GN_H, B.h0, GN_ENC, s0, s1, grad + OFF_W1, GN_ENC, GN_H, overflow);
+	wgrad_layer<4, 8>(B.d[1], GN_H, B.h[0], GN_H, s0, s1, grad + OFF_W2, GN_H, GN_H, overflow);
+	wgrad_layer<4, 8>(B.d[2], GN_H, B.h[1], GN_H, s0, s1, grad + OFF_W3, GN_H, GN_H, overflow);
+	wgrad_layer<4, 8>(B.d[3], GN_H, B.h[2], GN_H, s0, s1, grad + OFF_W4, GN_H, GN_H, overflow);
+	wgrad_layer<3, 8>(B.d5, GN_OUT, B.h[3], GN_H, s0, s1, grad + OFF_W5, GN_H, 40, overflow);
+}
+
+__global__ void k_guide_bgrad(GuideTrainBufs B, int n, float *__restrict__ grad) {
+	int col = threadIdx.x;  // 0..303
+	if (col >= 4 * GN_H + GN_OUT) return;
+	int s0 = blockIdx.x * 1024, s1 = min(s0 + 1024, n);
+	float acc = 0.f;
+	if (col < 4 * GN_H) {
+		int L = col / GN_H, o = col - L * GN_H;
+		for (int s = s0; s < s1; ++s) acc += __half2float(B.d[L][(size_t)s * GN_H + o]);
+		int off = L == 0 ? OFF_B1 : L == 1 ? OFF_B2 : L == 2 ? OFF_B3 : OFF_B4;
+		atomicAdd(&grad[off + o], acc);
+	} else {
+		int o = col - 4 * GN_H;
+		if (o >= 40) return;
+		for (int s = s0; s < s1; ++s) acc += __half2float(B.d5[(size_t)s * GN_OUT + o]);
+		atomicAdd(&grad[OFF_B5 + o], acc);
+	}
+}
+
+__global__ void k_guide_adam(float *__restrict__ P, float *__restrict__ m, float *__restrict__ v,
+	const float *__restrict__ grad, float gscale, float lr, float b1, float b2, float eps, float c1, float c2,
+	const unsigned *overflow) {
+	if (*overflow) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < GN_PARAMS; i += gridDim.x * blockDim.x) {
+		float gi = grad[i] * gscale;
+		float mi = b1 * m[i] + (1.f - b1) * gi;
+		float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+		m[i] = mi;
+		v[i] = vi;
+		P[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+	}
+}
+
+// n / (sum of the batch's weights) -> *out
+__global__ void k_weight_scale(const float *__restrict__ samples, int n, float *__restrict__ out) {
+	__shared__ float red[256];
+	float acc = 0.f;
+	for (int i = threadIdx.x; i < n; i += blockDim.x) acc += samples[(size_t)i * 16 + 12];
+	red[threadIdx.x] = acc;
+	__syncthreads();
+	for (int w = 128; w > 0; w >>= 1) {
+		if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) *out = red[0] > 0.f ? (float)n / red[0] : 0.f;
+}
+
+__global__ void k_scale_copy(const float *__restrict__ g, float s, float *__restrict__ out, int n) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = g[i] * s;
+}
+
+are_status bad(const std::string &m) {
+	set_error(m);
+	return ARE_ERR_INVALID_ARGUMENT;
+}
+
+}  // namespace
+
+size_t guide_infer_smem() { return IMG_FWD * sizeof(__half) + IMG_BIAS * sizeof(float); }
+size_t guide_train_smem() {
+	return IMG_ALL * sizeof(__half) + IMG_BIAS * sizeof(float) + (GT / 32) * 16 * GN_OUT * sizeof(float) +
+		(GT / 32) * 16 * S_OUT * sizeof(__half);
+}
+
+GuideNet::~GuideNet() {
+	if (stream) cudaStreamSynchronize(stream);
+	for (void *p : allocs) cudaFree(p);
+	if (train_mem) cudaFree(train_mem);
+	if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+are_status GuideNet::init(uint64_t seed) {
+	cudaGetDevice(&device);
+	cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, device);
+	if (are_status st = cuda_status(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate")) return st;
+	own_stream = true;
+	auto alloc = [&](void **p, size_t bytes) -> are_status {
+		if (are_status st = cuda_status(cudaMalloc(p, bytes), "cudaMalloc(guide)")) return st;
+		allocs.push_back(*p);
+		return cuda_status(cudaMemset(*p, 0, bytes), "cudaMemset(guide)");
+	};
+	if (are_status st = alloc((void **)&params, GN_PARAMS * sizeof(float))) return st;
+	if (are_status st = alloc((void **)&adam_m, GN_PARAMS * sizeof(float))) return st;
+	if (are_status st = alloc((void **)&adam_v, GN_PARAMS * sizeof(float))) return st;
+	if (are_status st = alloc((void **)&grad, (GN_PARAMS + 64) * sizeof(float))) return st;
+	if (are_status st = alloc((void **)&img, IMG_ALL * sizeof(__half))) return st;
+	if (are_status st = alloc((void **)&bias, IMG_BIAS * sizeof(float))) return st;
+	if (cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_infer_smem()) != cudaSuccess ||
+		cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_train_smem()) != cudaSuccess)
+		return cuda_status(cudaGetLastError(), "cudaFuncSetAttribute(guide)");
+	// seeded He-uniform initialisation on the host (SplitMix64 stream)
+	std::vector<float> h(GN_PARAMS, 0.0f);
+	uint64_t s = seed;
+	auto unif = [&]() {
+		uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+		z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+		z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+		z ^= z >> 31;
+		return (double)(z >> 11) * 0x1.0p-53;
+	};
+	auto fill = [&](int off, int rows, int cols, double bound) {
+		for (int r = 0; r < rows; ++r)
+			for (int c = 0; c < cols; ++c) h[off + r * cols + c] = (float)((2.0 * unif() - 1.0) * bound);
+	};
+	fill(OFF_W1, GN_H, GN_ENC, std::sqrt(6.0 / 225.0));
+	fill(OFF_W2, GN_H, GN_H, std::sqrt(6.0 / GN_H));
+	fill(OFF_W3, GN_H, GN_H, std::sqrt(6.0 / GN_H));
+	fill(OFF_W4, GN_H, GN_H, std::sqrt(6.0 / GN_H));
+	fill(OFF_W5, 40, GN_H, 0.1 * std::sqrt(3.0 / GN_H));
+	return set_params(h.data());
+}
+
+are_status GuideNet::set_params(const float *host) {
+	if (are_status st = cuda_status(cudaMemcpyAsync(params, host, GN_PARAMS * sizeof(float), cudaMemcpyHostToDevice, stream), "H2D params"))
+		return st;
+	cudaMemsetAsync(adam_m, 0, GN_PARAMS * sizeof(float), stream);
+	cudaMemsetAsync(adam_v, 0, GN_PARAMS * sizeof(float), stream);
+	steps = 0;
+	return pack();
+}
+
+are_status GuideNet::pack() {
+	k_guide_pack<<<128, 256, 0, stream>>>(params, img, bias);
+	return cuda_status(cudaGetLastError(), "k_guide_pack");
+}
+
+are_status GuideNet::ensure_train(int n) {
+	int cap = (n + 15) & ~15;
+	if (cap <= train_cap) return ARE_OK;
+	if (train_mem) cudaFree(train_mem);
+	train_mem = nullptr;
+	train_cap = 0;
+	size_t per = (size_t)(GN_ENC + 8 * GN_H + GN_OUT) * sizeof(__half);
+	if (are_status st = cuda_status(cudaMalloc(&train_mem, per * cap + 16 * GN_ENC * sizeof(__half) + 1024), "cudaMalloc(guide training)"))
+		return st;
+	__half *p = (__half *)train_mem;
+	bufs.h0 = p, p += (size_t)(cap + 16) * GN_ENC;
+	bufs.dump_row = cap;
+	for (int L = 0; L < 4; ++L) bufs.h[L] = p, p += (size_t)cap * GN_H;
+	for (int L = 0; L < 4; ++L) bufs.d[L] = p, p += (size_t)cap * GN_H;
+	bufs.d5 = p;
+	train_cap = cap;
+	return ARE_OK;
+}
+
+are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev) {
+	if (n <= 0) return ARE_OK;
+	int per_sm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_guide_infer, GT, guide_infer_smem());
+	int grid = std::max(1, per_sm) * n_sms;
+	grid = std::min(grid, ((n + 15) / 16 + 7) / 8);
+	k_guide_infer<<<grid, GT, guide_infer_smem(), s>>>(img, bias, d_feat, n, n_dev, d_out);
+	return cuda_status(cudaGetLastError(), "k_guide_infer");
+}
+
+// samples: n x 16 device floats (features 9, direction 3, weight 1, 3 unused).
+// Accumulates the gradient (FP32, times the loss scale) in `grad` and the loss in grad[GN_PARAMS].
+are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaStream_t s) {
+	if (are_status st = ensure_train(n)) return st;
+	int np = (n + 15) & ~15;
+	cudaMemsetAsync(grad, 0, (GN_PARAMS + 64) * sizeof(float), s);
+	// rows n..np-1 of the training buffers are zero gradients
+	if (np > n) {
+		for (int L = 0; L < 4; ++L) {
+			cudaMemsetAsync(bufs.d[L] + (size_t)n * GN_H, 0, (size_t)(np - n) * GN_H * 2, s);
+			cudaMemsetAsync(bufs.h[L] + (size_t)n * GN_H, 0, (size_t)(np - n) * GN_H * 2, s);
+		}
+		cudaMemsetAsync(bufs.d5 + (size_t)n * GN_OUT, 0, (size_t)(np - n) * GN_OUT * 2, s);
+		cudaMemsetAsync(bufs.h0 + (size_t)n * GN_ENC, 0, (size_t)(np - n) * GN_ENC * 2, s);
+	}
+	int tiles = np / 16;
+	int grid = std::max(1, std::min(n_sms, (tiles + 7) / 8));
+	// wmean < 0: the batch's mean weight is computed on the device
+	const float *wdev = nullptr;
+	float wscale = wmean > 0.f ? 1.0f / wmean : 0.f;
+	if (wmean < 0.f) {
+		k_weight_scale<<<1, 256, 0, s>>>(d_samples, n, grad + GN_PARAMS + 2);
+		wdev = grad + GN_PARAMS + 2;
+	}
+	k_guide_fwdbwd<<<grid, GT, guide_train_smem(), s>>>(img, bias, d_samples, n, wscale, wdev, weight_clip, loss_scale,
+		bufs, grad + GN_PARAMS);
+	k_guide_wgrad<<<(np + WG_CHUNK - 1) / WG_CHUNK, GT, 0, s>>>(bufs, np, grad, (unsigned *)(grad + GN_PARAMS + 1));
+	k_guide_bgrad<<<(np + 1023) / 1024, 320, 0, s>>>(bufs, np, grad);
+	return cuda_status(cudaGetLastError(), "guide gradient kernels");
+}
+
+are_status GuideNet::train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s) {
+	if (are_status st = gradient(d_samples, n, wmean, s)) return st;
+	++steps;
+	float c1 = 1.f - std::pow(0.9f, (float)steps), c2 = 1.f - std::pow(0.99f, (float)steps);
+	k_guide_adam<<<64, 256, 0, s>>>(params, adam_m, adam_v, grad, 1.0f / (loss_scale * (float)n), lr, 0.9f, 0.99f, 1e-8f,
+		c1, c2, (const unsigned *)(grad + GN_PARAMS + 1));
+	k_guide_pack<<<128, 256, 0, s>>>(params, img, bias);
+	return cuda_status(cudaGetLastError(), "guide Adam");
+}
+
+}  // namespace are_core
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+using are_core::GuideNet;
+
+namespace {
+template <class F>
+are_status guard(F &&f) {
+	try {
+		are_core::set_error("");
+		return f();
+	} catch (const std::bad_alloc &) {
+		are_core::set_error("out of host memory");
+		return ARE_ERR_OUT_OF_MEMORY;
+	} catch (...) {
+		are_core::set_error("unexpected exception");
+		return ARE_ERR_INTERNAL;
+	}
+}
+
+// host buffer -> device scratch of the net's stream, freed after use
+struct DevTmp {
+	void *p = nullptr;
+	~DevTmp() {
+		if (p) cudaFree(p);
+	}
+};
+}  // namespace
+
+extern "C" {
+
+ARE_API int32_t are_guide_param_count(void) { return are_core::GN_PARAMS; }
+
+ARE_API are_status are_guide_create(uint64_t seed, are_guide **out) {
+	return guard([&] {
+		if (!out) return are_core::bad("null output");
+		*out = nullptr;
+		int n = 0;
+		if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+			cudaGetLastError();
+			are_core::set_error("no CUDA device");
+			return ARE_ERR_NO_DEVICE;
+		}
+		GuideNet *g = new GuideNet();
+		if (are_status st = g->init(seed)) {
+			delete g;
+			return st;
+		}
+		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide init")) {
+			delete g;
+			return st;
+		}
+		*out = reinterpret_cast<are_guide *>(g);
+		return ARE_OK;
+	});
+}
+
+ARE_API are_status are_guide_destroy(are_guide *g) {
+	return guard([&] {
+		delete reinterpret_cast<GuideNet *>(g);
+		return ARE_OK;
+	});
+}
+
+ARE_API are_status are_guide_get_params(are_guide *gh, float *out) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || !out) return are_core::bad("null guide or output");
+		cudaMemcpyAsync(out, g->params, are_core::GN_PARAMS * sizeof(float), cudaMemcpyDeviceToHost, g->stream);
+		return are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide params");
+	});
+}
+
+ARE_API are_status are_guide_set_params(are_guide *gh, const float *in) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || !in) return are_core::bad("null guide or input");
+		if (are_status st = g->set_params(in)) return st;
+		return are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide params");
+	});
+}
+
+ARE_API are_status are_guide_forward(are_guide *gh, const float *features, int64_t n, float *out) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || (n > 0 && (!features || !out)) || n < 0 || n > (1 << 26)) return are_core::bad("bad guide forward arguments");
+		if (n == 0) return ARE_OK;
+		DevTmp t;
+		size_t fb = (size_t)n * are_core::GN_IN * 4, ob = (size_t)n * are_core::GN_OUT * 4;
+		if (are_status st = are_core::cuda_status(cudaMalloc(&t.p, fb + ob), "cudaMalloc")) return st;
+		cudaMemcpyAsync(t.p, features, fb, cudaMemcpyHostToDevice, g->stream);
+		if (are_status st = g->infer((const float *)t.p, (int)n, (float *)((char *)t.p + fb), g->stream)) return st;
+		cudaMemcpyAsync(out, (char *)t.p + fb, ob, cudaMemcpyDeviceToHost, g->stream);
+		return are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide forward");
+	});
+}
+
+// samples: n x 13 host floats (features 9, direction 3, weight 1)
+static are_status upload_samples(GuideNet *g, const float *samples, int64_t n, DevTmp &t, float &wmean) {
+	std::vector<float> s16((size_t)n * 16, 0.0f);
+	double ws = 0.0;
+	for (int64_t i = 0; i < n; ++i) {
+		std::memcpy(&s16[(size_t)i * 16], samples + 13 * i, 13 * sizeof(float));
+		ws += samples[13 * i + 12];
+	}
+	wmean = n > 0 ? (float)(ws / (double)n) : 0.f;
+	if (are_status st = are_core::cuda_status(cudaMalloc(&t.p, s16.size() * 4), "cudaMalloc")) return st;
+	cudaMemcpyAsync(t.p, s16.data(), s16.size() * 4, cudaMemcpyHostToDevice, g->stream);
+	return are_core::cuda_status(cudaStreamSynchronize(g->stream), "upload samples");
+}
+
+ARE_API are_status are_guide_gradient(are_guide *gh, const float *samples, int64_t n, float *loss, float *grad) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || !samples || !grad || n <= 0 || n > (1 << 22)) return are_core::bad("bad guide gradient arguments");
+		DevTmp t;
+		float wmean = 0.f;
+		if (are_status st = upload_samples(g, samples, n, t, wmean)) return st;
+		if (are_status st = g->gradient((const float *)t.p, (int)n, wmean, g->stream)) return st;
+		std::vector<float> h(are_core::GN_PARAMS + 2);
+		cudaMemcpyAsync(h.data(), g->grad, h.size() * 4, cudaMemcpyDeviceToHost, g->stream);
+		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide gradient")) return st;
+		float s = 1.0f / (g->loss_scale * (float)n);
+		for (int i = 0; i < are_core::GN_PARAMS; ++i) grad[i] = h[i] * s;
+		if (loss) *loss = h[are_core::GN_PARAMS] / (float)n;
+		unsigned of;
+		std::memcpy(&of, &h[are_core::GN_PARAMS + 1], 4);
+		if (of) {
+			are_core::set_error("FP16 overflow in the backward pass");
+			return ARE_ERR_INTERNAL;
+		}
+		return ARE_OK;
+	});
+}
+
+ARE_API are_status are_render_guided(are_scene *scene, are_guide *guide, const are_camera *camera,
+	const are_render_params *params, const are_guide_params *guide_params, float *rgb_out, float *var_out,
+	are_render_stats *stats) {
+	return guard([&] {
+		return are_core::render_guided(scene, reinterpret_cast<GuideNet *>(guide), camera, params, guide_params, rgb_out,
+			var_out, stats);
+	});
+}
+
+ARE_API int32_t are_guide_loss_history(are_guide *gh, float *out, int32_t max) {
+	GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+	if (!g || !out || max <= 0) return 0;
+	int32_t n = (int32_t)std::min<size_t>((size_t)max, g->loss_log.size());
+	std::memcpy(out, g->loss_log.data() + (g->loss_log.size() - n), n * sizeof(float));
+	return n;
+}
+
+ARE_API are_status are_guide_train(are_guide *gh, const float *samples, int64_t n, float lr, float *loss) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || !samples || n <= 0 || n > (1 << 22) || !(lr > 0.f)) return are_core::bad("bad guide train arguments");
+		DevTmp t;
+		float wmean = 0.f;
+		if (are_status st = upload_samples(g, samples, n, t, wmean)) return st;
+		if (are_status st = g->train_step((const float *)t.p, (int)n, wmean, lr, g->stream)) return st;
+		float l = 0.f;
+		cudaMemcpyAsync(&l, g->grad + are_core::GN_PARAMS, 4, cudaMemcpyDeviceToHost, g->stream);
+		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide train")) return st;
+		if (loss) *loss = l / (float)n;
+		return ARE_OK;
+	});
+}
+
+}  // extern "C"

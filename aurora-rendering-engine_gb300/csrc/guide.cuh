@@ -1,0 +1,178 @@
+// guide.cuh — the path-guiding network on the device: layout constants,
+// input encoding, the von Mises-Fisher mixture it outputs, and the tensor-core
+// building blocks of its fused forward/backward kernels.
+//
+// The network and its loss are specified in oracle/orc_guide.c (FP64); the
+// device computes the same in FP16 on the tensor cores with FP32
+// accumulation (mma.sync.m16n8k16, activations kept in registers between
+// layers as in the fully fused MLPs of Mueller et al., "Real-time Neural
+// Radiance Caching", 2021), FP32 master weights and Adam.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace are_core {
+
+constexpr int GN_IN = 9, GN_ENC = 256, GN_H = 64, GN_OUT = 48, GN_LOBES = 8;
+// flat FP32 parameters, rows [out][in] (as the oracle)
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + GN_H * GN_ENC;
+constexpr int OFF_W2 = OFF_B1 + GN_H, OFF_B2 = OFF_W2 + GN_H * GN_H;
+constexpr int OFF_W3 = OFF_B2 + GN_H, OFF_B3 = OFF_W3 + GN_H * GN_H;
+constexpr int OFF_W4 = OFF_B3 + GN_H, OFF_B4 = OFF_W4 + GN_H * GN_H;
+constexpr int OFF_W5 = OFF_B4 + GN_H, OFF_B5 = OFF_W5 + GN_OUT * GN_H;
+constexpr int GN_PARAMS = OFF_B5 + GN_OUT;
+
+// FP16 weight image, copied whole into shared memory.  Row strides are padded
+// by 8 halves so the B-fragment loads of a warp hit 32 distinct banks.
+constexpr int S_ENC = GN_ENC + 8, S_H = GN_H + 8, S_OUT = GN_OUT + 8;
+constexpr int IMG_W1 = 0;                          // [64][S_ENC]   forward
+constexpr int IMG_W2 = IMG_W1 + GN_H * S_ENC;      // [64][S_H]
+constexpr int IMG_W3 = IMG_W2 + GN_H * S_H;
+constexpr int IMG_W4 = IMG_W3 + GN_H * S_H;
+constexpr int IMG_W5 = IMG_W4 + GN_H * S_H;        // [48][S_H]
+constexpr int IMG_FWD = IMG_W5 + GN_OUT * S_H;     // halves of the forward image
+constexpr int IMG_W2T = IMG_FWD;                   // [64 in][S_H] transposed, backward
+constexpr int IMG_W3T = IMG_W2T + GN_H * S_H;
+constexpr int IMG_W4T = IMG_W3T + GN_H * S_H;
+constexpr int IMG_W5T = IMG_W4T + GN_H * S_H;      // [64 in][S_OUT]
+constexpr int IMG_ALL = IMG_W5T + GN_H * S_OUT;    // halves of forward + backward image
+constexpr int IMG_BIAS = 4 * GN_H + GN_OUT;        // FP32 biases after the halves
+
+// features of a shading point: position scaled to the scene box, normal, outgoing direction
+struct GuideBox {
+	float lo[3], inv_ext[3];
+};
+
+__device__ __forceinline__ void guide_features(const GuideBox &B, f3 p, f3 n, f3 wo, float *x) {
+	x[0] = 2.0f * (p.x - B.lo[0]) * B.inv_ext[0] - 1.0f;
+	x[1] = 2.0f * (p.y - B.lo[1]) * B.inv_ext[1] - 1.0f;
+	x[2] = 2.0f * (p.z - B.lo[2]) * B.inv_ext[2] - 1.0f;
+	x[3] = n.x, x[4] = n.y, x[5] = n.z;
+	x[6] = wo.x, x[7] = wo.y, x[8] = wo.z;
+}
+
+// encoding pair index 0..127 -> two consecutive encoding values
+__device__ __forceinline__ __half2 enc_pair(const float *x, int pi) {
+	if (pi < 108) {
+		int i = pi / 12, k = pi - 12 * (pi / 12);
+		float s, c;
+		sincospif(ldexpf(x[i], k), &s, &c);
+		return __floats2half2_rn(s, c);
+	}
+	if (pi < 113) {
+		int m = 2 * (pi - 108);
+		return __floats2half2_rn(x[m], m + 1 < GN_IN ? x[m + 1] : 0.0f);
+	}
+	return __floats2half2_rn(0.0f, 0.0f);
+}
+
+__device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t *>(&h); }
+__device__ __forceinline__ __half2 u2h(uint32_t u) { return *reinterpret_cast<__half2 *>(&u); }
+
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b0, uint32_t b1) {
+	asm volatile(
+		"mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+		"{%0,%1,%2,%3};\n"
+		: "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+		: "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// One dense layer on a 16-row tile: C[nt] (16 x 8 per n-tile) += A (16 x K) W^T
+// with W an [out][in] half matrix of row stride `stride` in shared memory.
+// A is given as K/16 groups of 4 fragment registers.
+template <int KSTEPS, int NTILES>
+__device__ __forceinline__ void tile_layer(const uint32_t (*a)[4], const __half *W, int stride, float (*c)[4]) {
+	const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+#pragma unroll
+	for (int nt = 0; nt < NTILES; ++nt) {
+		c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
+		const __half *row = W + (nt * 8 + g) * stride + 2 * t;
+#pragma unroll
+		for (int ks = 0; ks < KSTEPS; ++ks) {
+			uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + ks * 16);
+			uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + ks * 16 + 8);
+			mma16816(c[nt], a[ks], b0, b1);
+		}
+	}
+}
+
+// C fragments of a 16 x 64 layer (+bias, ReLU) -> A fragments of the next layer.
+__device__ __forceinline__ void relu_to_a(float (*c)[4], const float *bias, uint32_t (*a)[4]) {
+	const int t = threadIdx.x & 3;
+#pragma unroll
+	for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			int nt = 2 * ks + h;
+			float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
+			float v0 = fmaxf(c[nt][0] + b0, 0.f), v1 = fmaxf(c[nt][1] + b1, 0.f);
+			float v2 = fmaxf(c[nt][2] + b0, 0.f), v3 = fmaxf(c[nt][3] + b1, 0.f);
+			a[ks][2 * h] = h2u(__floats2half2_rn(v0, v1));
+			a[ks][2 * h + 1] = h2u(__floats2half2_rn(v2, v3));
+		}
+	}
+}
+
+// ---- the vMF mixture -------------------------------------------------------
+
+struct Mixture {
+	f3 mu[GN_LOBES];
+	float kappa[GN_LOBES], pi[GN_LOBES], norm[GN_LOBES];  // norm = kappa / (2 pi (1 - e^-2kappa))
+};
+
+__device__ __forceinline__ float softplusf(float x) { return x > 20.f ? x : log1pf(__expf(x)); }
+
+__device__ __forceinline__ void to_mixture(const float *o, Mixture &m) {
+	float mx = -1e30f;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) mx = fmaxf(mx, o[5 * l + 4]);
+	float z = 0.f;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) {
+		float len = sqrtf(o[5 * l] * o[5 * l] + o[5 * l + 1] * o[5 * l + 1] + o[5 * l + 2] * o[5 * l + 2]) + 1e-6f;
+		m.mu[l] = f3{ o[5 * l] / len, o[5 * l + 1] / len, o[5 * l + 2] / len };
+		float k = softplusf(o[5 * l + 3]) + 0.05f;
+		m.kappa[l] = k;
+		m.norm[l] = k / (6.28318530717958647692f * -expm1f(-2.f * k));
+		m.pi[l] = __expf(o[5 * l + 4] - mx);
+		z += m.pi[l];
+	}
+	float iz = 1.f / z;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) m.pi[l] *= iz;
+}
+
+__device__ __forceinline__ float mixture_pdf(const Mixture &m, f3 w) {
+	float q = 0.f;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) {
+		float c = m.mu[l].x * w.x + m.mu[l].y * w.y + m.mu[l].z * w.z;
+		q += m.pi[l] * m.norm[l] * __expf(m.kappa[l] * (c - 1.f));
+	}
+	return q;
+}
+
+// Draw a direction: lobe by u0, then the vMF sample of W. Jakob's stable form
+// cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) / kappa, azimuth 2 pi u2.
+__device__ __forceinline__ f3 mixture_sample(const Mixture &m, float u0, float u1, float u2) {
+	int l = 0;
+	float acc = m.pi[0];
+	while (l < GN_LOBES - 1 && u0 >= acc) acc += m.pi[++l];
+	float k = m.kappa[l];
+	float w = 1.f + logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k;
+	w = fminf(fmaxf(w, -1.f), 1.f);
+	float r = sqrtf(fmaxf(0.f, 1.f - w * w));
+	float s, c;
+	sincospif(2.f * u2, &s, &c);
+	f3 z = m.mu[l];
+	f3 up = fabsf(z.z) < 0.999f ? f3{ 0.f, 0.f, 1.f } : f3{ 1.f, 0.f, 0.f };
+	f3 x = norm(cross(z, up));
+	f3 y = cross(z, x);
+	return norm(add(add(scl(x, r * c), scl(y, r * s)), scl(z, w)));
+}
+
+}  // namespace are_core

@@ -1,0 +1,60 @@
+// guide_host.h — host-side owner of a path-guiding network (the opaque
+// are_guide of the C ABI): FP32 master parameters, Adam moments, the FP16
+// weight image the kernels load, and the training buffers.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "aurora_gb300.h"
+
+namespace are_core {
+
+// per-sample tensors of one training batch, FP16 [samples][features]
+struct GuideTrainBufs {
+	__half *h0;     // encoded inputs [cap + 16][256] (row cap+ is a write-only dump row)
+	__half *h[4];   // hidden outputs h1..h4 [cap][64]
+	__half *d[4];   // gradients at h1..h4 pre-activations [cap][64]
+	__half *d5;     // output gradients [cap][48]
+	int dump_row;
+};
+
+struct GuideNet {
+	int device = 0, n_sms = 0;
+	cudaStream_t stream = nullptr;
+	bool own_stream = false;
+	float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+	float *grad = nullptr;  // GN_PARAMS gradients, then loss sum, then an overflow flag
+	__half *img = nullptr;
+	float *bias = nullptr;
+	void *train_mem = nullptr;
+	int train_cap = 0;
+	GuideTrainBufs bufs{};
+	std::vector<void *> allocs;
+	int64_t steps = 0;
+	float loss_scale = 8.0f;     // gradients are carried in FP16 times this factor
+	float weight_clip = 1e30f;   // cap on a sample's normalised weight
+	std::vector<float> loss_log; // losses of Adam steps taken inside renders
+
+	~GuideNet();
+	are_status init(uint64_t seed);
+	are_status set_params(const float *host);
+	are_status pack();
+	are_status ensure_train(int n);
+	// n_dev: optional device row count (rows = min(n, *n_dev)), read when the kernel runs
+	are_status infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev = nullptr);
+	// wmean < 0: normalise the weights by their batch mean computed on the device
+	are_status gradient(const float *d_samples, int n, float wmean, cudaStream_t s);
+	are_status train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s);
+};
+
+size_t guide_infer_smem();
+size_t guide_train_smem();
+
+are_status render_guided(struct ::are_scene *sc, GuideNet *net, const are_camera *cam, const are_render_params *prm,
+	const are_guide_params *gp, float *rgb, float *var, are_render_stats *stats);
+
+}  // namespace are_core

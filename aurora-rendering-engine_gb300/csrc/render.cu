@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 		float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
 		Hit h;
 		if (linear) {
-			h = closest_hit_linear(snodes, S.n_prims, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w);
+			h = closest_hit_linear(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w);
 		} else {
 			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
 		}
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 	const float inf = __int_as_float(0x7f800000);
 	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		float4 r0 = qa[i], r1 = qb[i];
-		Hit h = linear ? closest_hit_linear(snodes, S.n_prims, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf)
+		Hit h = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf)
 					   : closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
 		W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}

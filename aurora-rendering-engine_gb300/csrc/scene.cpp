@@ -207,6 +207,15 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	if (!st) st = upload(sc, mat.data(), mat.size(), &S.prim_mat);
 	if (!st) st = upload(sc, tri_uv.data(), tri_uv.size(), &S.tri_uv);
 	if (!st) st = upload(sc, (const float4 *)bvh.nodes.data(), bvh.nodes.size() / 4, &np);
+	std::vector<float> leaves;
+	if (n > 0 && n <= LINEAR_MAX)
+		for (int32_t i = 0; i < bvh.n_nodes; ++i) {
+			int32_t cnt;
+			std::memcpy(&cnt, &bvh.nodes[8 * (size_t)i + 7], 4);
+			if (cnt > 0) leaves.insert(leaves.end(), &bvh.nodes[8 * (size_t)i], &bvh.nodes[8 * (size_t)i] + 8);
+		}
+	const float4 *lp = nullptr;
+	if (!st) st = upload(sc, (const float4 *)leaves.data(), leaves.size() / 4, &lp);
 	if (!st) st = upload(sc, (const DevMaterial *)d->materials, (size_t)d->n_materials, &S.mats);
 	if (!st) st = upload(sc, (const DevTexture *)d->textures, (size_t)d->n_textures, &S.texs);
 	if (!st) st = upload(sc, d->texels, 3 * (size_t)d->n_texels, &S.texels);
@@ -218,6 +227,8 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	}
 	S.prims = pp;
 	S.nodes = np;
+	S.leaves = lp;
+	S.n_leaves = (int32_t)(leaves.size() / 8);
 	S.n_prims = n;
 	S.n_nodes = bvh.n_nodes;
 	S.n_materials = d->n_materials;
@@ -228,6 +239,11 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	S.box_pad = bvh.box_pad;
 	sc->n_prims = n;
 	sc->n_spheres = ns, sc->n_quads = nq, sc->n_triangles = nt;
+	for (int k = 0; k < 3; ++k) {
+		double lo = n ? boxes[0].lo[k] : 0.0, hi = n ? boxes[0].hi[k] : 0.0;
+		for (const PrimBox &b : boxes) lo = std::fmin(lo, b.lo[k]), hi = std::fmax(hi, b.hi[k]);
+		sc->box_lo[k] = (float)lo, sc->box_hi[k] = (float)hi;
+	}
 	sc->n_nodes = bvh.n_nodes;
 	sc->max_leaf = bvh.max_leaf;
 	sc->depth = bvh.depth;

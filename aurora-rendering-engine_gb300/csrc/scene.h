@@ -17,6 +17,7 @@ struct are_scene {
 	int64_t n_prims = 0, n_nodes = 0;
 	int32_t n_spheres = 0, n_quads = 0, n_triangles = 0;
 	int32_t max_leaf = 0, depth = 0;
+	float box_lo[3] = { 0, 0, 0 }, box_hi[3] = { 0, 0, 0 };  // bounds of all primitives
 	std::vector<void *> allocations;  // device buffers owned by the scene
 	cudaStream_t stream = nullptr;
 
@@ -44,6 +45,10 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	are_render_stats *stats);
 are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
 	are_render_stats *stats);
+are_status render_batch(are_scene *const *scenes, const are_camera *cams, const are_render_params *params, int n,
+	const are_batch_options *opt, float *const *rgb_out, double *scene_ms, are_render_stats *stats);
+are_status batch_autotune(const are_scene_desc *const *descs, const are_camera *cams, const are_render_params *params,
+	int n, int calib_spp, are_batch_options *best, double *best_ms);
 are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_params &p, float *rgb,
 	are_render_stats *stats);
 are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms);

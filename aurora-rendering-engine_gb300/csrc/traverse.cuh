@@ -72,6 +72,8 @@ __device__ __forceinline__ bool hit_sphere(float4 s0, f3 o, f3 d, float tmin, fl
 // Quad (Q, u, v): plane hit (src/basic/plane.cpp:13-27), then the planar
 // coordinates alpha, beta in [0,1]^2.  New primitive.
 __device__ __forceinline__ bool quad_t_reject(float num, float denom, float tmin, float tcut);
+__device__ __forceinline__ bool coord_reject(float na, float nn);
+__device__ __forceinline__ bool coord_inside(float na, float nn);
 
 __device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmin, float tmax, float tcut,
 	float &tout, float &uo, float &vo) {
@@ -84,9 +86,12 @@ __device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmi
 	if (!(t > tmin && t < tmax)) return false;
 	f3 p = rsub(radd(o, rscl(d, t)), Q);
 	float nn = rdot(n, n);
-	float al = __fdiv_rn(rdot(n, rcross(p, v)), nn);
-	float be = __fdiv_rn(rdot(n, rcross(u, p)), nn);
-	if (!(al >= 0.0f && al <= 1.0f && be >= 0.0f && be <= 1.0f)) return false;
+	float na = rdot(n, rcross(p, v));
+	if (!coord_inside(na, nn)) return false;
+	float nb = rdot(n, rcross(u, p));
+	if (!coord_inside(nb, nn)) return false;
+	float al = __fdiv_rn(na, nn);
+	float be = __fdiv_rn(nb, nn);
 	tout = t;
 	uo = al;
 	vo = be;
@@ -108,6 +113,27 @@ __device__ __forceinline__ bool quad_t_reject(float num, float denom, float tmin
 	return lim >= 1.17549435e-38f && fabsf(num) > lim;
 }
 
+// With nn >= 2^-60 the rounded quotient q = na / nn lies outside [0, 1]
+// whenever na < -nn 2^-60 (then q < -2^-60) or na > fl(nn (1 + 2^-21)) (then
+// q > 1 + 2^-22, which rounds above 1); both thresholds are normal floats, the
+// first exact.  Those coordinates are rejected without dividing; borderline
+// cases and tiny quads divide, so no answer changes.
+__device__ __forceinline__ bool coord_reject(float na, float nn) {
+	if (!(na == na)) return true;
+	if (!(nn >= 8.67361738e-19f)) return false;
+	return na < -nn * 8.67361738e-19f || na > nn * 1.00000047683716f;
+}
+
+// The same decision as fl(na / nn) in [0, 1] (nn > 0), dividing only in the
+// borderline bands: 0 <= na <= fl(nn (1 - 2^-23)) means q <= 1 - 2^-24, which
+// rounds to at most 1, so it is inside; coord_reject covers the clear outside.
+__device__ __forceinline__ bool coord_inside(float na, float nn) {
+	if (coord_reject(na, nn)) return false;
+	if (nn >= 8.67361738e-19f && na >= 0.0f && na <= nn * 0.99999988079071f) return true;
+	float q = __fdiv_rn(na, nn);
+	return q >= 0.0f && q <= 1.0f;
+}
+
 __device__ __forceinline__ bool hit_quad_pre(f3 Q, f3 u, f3 v, f3 n, float nn, f3 o, f3 d, float tmin, float tmax,
 	float tcut, float &tout, float &uo, float &vo) {
 	float denom = rdot(n, d);
@@ -117,13 +143,14 @@ __device__ __forceinline__ bool hit_quad_pre(f3 Q, f3 u, f3 v, f3 n, float nn, f
 	float t = __fdiv_rn(num, denom);
 	if (!(t > tmin && t < tmax)) return false;
 	f3 p = rsub(radd(o, rscl(d, t)), Q);
-	float al = __fdiv_rn(rdot(n, rcross(p, v)), nn);
-	if (!(al >= 0.0f && al <= 1.0f)) return false;
-	float be = __fdiv_rn(rdot(n, rcross(u, p)), nn);
-	if (!(be >= 0.0f && be <= 1.0f)) return false;
+	float na = rdot(n, rcross(p, v));
+	if (!coord_inside(na, nn)) return false;
+	float nb = rdot(n, rcross(u, p));
+	if (!coord_inside(nb, nn)) return false;
+	// uo/vo carry the numerators; the caller divides by nn for the final hit only
 	tout = t;
-	uo = al;
-	vo = be;
+	uo = na;
+	vo = nb;
 	return true;
 }
 
@@ -198,8 +225,10 @@ __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
 // Stages the primitives of a scene with at most LINEAR_MAX of them into
 // shared memory: per primitive [0..2] the leaf-order record (global id in
-// [1].w), [3] the quad normal u x v and its squared length.
+// [1].w), [3] the quad normal u x v and its squared length; then, from
+// sp[4 LINEAR_MAX] on, the BVH's leaf boxes (2 float4 each, node format).
 __device__ __forceinline__ void stage_prims(const DevScene &S, float4 *sp) {
+	for (int l = threadIdx.x; l < 2 * S.n_leaves; l += blockDim.x) sp[4 * LINEAR_MAX + l] = __ldg(S.leaves + l);
 	for (int j = threadIdx.x; j < S.n_prims; j += blockDim.x) {
 		const float4 *P = S.prims + 3 * (size_t)j;
 		float4 p0 = __ldg(P), p1 = __ldg(P + 1), p2 = __ldg(P + 2);
@@ -217,24 +246,43 @@ __device__ __forceinline__ void stage_prims(const DevScene &S, float4 *sp) {
 // strategy (rt.cpp:209-218).  Every lane of a warp walks the same primitive
 // at the same time, so the loads are shared-memory broadcasts and the control
 // flow only diverges inside a primitive test.  Same answer as closest_hit.
-__device__ __forceinline__ Hit closest_hit_linear(const float4 *__restrict__ sp, int n, int tri_wt, f3 o, f3 d,
+__device__ __forceinline__ Hit closest_hit_linear(const float4 *__restrict__ sp, int n_leaves, int tri_wt, f3 o, f3 d,
 	float tmin, float tmax) {
 	Hit best;
 	best.t = __int_as_float(0x7f800000);
 	best.leaf = -1;
 	best.gid = 0x7fffffff;
 	best.u = best.v = 0.0f;
-	for (int j = 0; j < n; ++j) {
+	float dx = d.x != 0.0f ? d.x : copysignf(1e-20f, d.x);
+	float dy = d.y != 0.0f ? d.y : copysignf(1e-20f, d.y);
+	float dz = d.z != 0.0f ? d.z : copysignf(1e-20f, d.z);
+	float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
+	float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+	float best_nn = 0.0f;  // quads report numerators; divided once for the final hit
+	for (int l = 0; l < n_leaves; ++l) {
+		// the leaf's padded box (culling only), then its primitives
+		float4 b0 = sp[4 * LINEAR_MAX + 2 * l], b1 = sp[4 * LINEAR_MAX + 2 * l + 1];
+		float t0x = fmaf(b0.x, ix, ox), t1x = fmaf(b1.x, ix, ox);
+		float t0y = fmaf(b0.y, iy, oy), t1y = fmaf(b1.y, iy, oy);
+		float t0z = fmaf(b0.z, iz, oz), t1z = fmaf(b1.z, iz, oz);
+		float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+		float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)),
+			fminf(fmaxf(t0z, t1z), fminf(best.t, tmax) * 1.0000039f));
+		if (!(lo <= hi)) continue;
+		const int first = __float_as_int(b0.w), end = first + __float_as_int(b1.w);
+	for (int j = first; j < end; ++j) {
 		float4 p0 = sp[4 * j];
 		float t, u = 0.0f, v = 0.0f;
 		bool h;
 		float4 p1 = sp[4 * j + 1];
+		float qnn = 0.0f;
 		if (p0.w > 0.0f) {
 			h = hit_sphere(p0, o, d, tmin, tmax, t);
 		} else {
 			float4 p2 = sp[4 * j + 2];
 			if (p0.w == PRIM_TAG_QUAD) {
 				float4 p3 = sp[4 * j + 3];
+				qnn = p3.w;
 				h = hit_quad_pre(ld3(p0), ld3(p1), ld3(p2), ld3(p3), p3.w, o, d, tmin, tmax, best.t, t, u, v);
 			} else if (tri_wt) {
 				h = hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
@@ -250,8 +298,14 @@ __device__ __forceinline__ Hit closest_hit_linear(const float4 *__restrict__ sp,
 				best.gid = gid;
 				best.u = u;
 				best.v = v;
+				best_nn = qnn;
 			}
 		}
+	}
+	}
+	if (best_nn != 0.0f) {
+		best.u = __fdiv_rn(best.u, best_nn);
+		best.v = __fdiv_rn(best.v, best_nn);
 	}
 	return best;
 }

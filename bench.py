@@ -142,6 +142,53 @@ def cpu_sample(scene, cam, par, budget_s: float, threads: int) -> dict:
             "segments": st["segments"]}
 
 
+def guiding_eval(budget_s: float = 0.1) -> dict | None:
+    """Equal-time relMSE of guided vs plain rendering on the occluded-light
+    Cornell box (200x200, depth 16) against the FP64 65,536-spp CPU reference
+    in tests/golden/guiding_reference_200.npz.  Each method gets the same
+    wall-clock budget for one render (the guided one trains its network online
+    inside that budget, from a fresh random initialisation)."""
+    import numpy as np
+
+    import are_gb300 as are
+
+    ref_path = REPO / "tests" / "golden" / "guiding_reference_200.npz"
+    if not ref_path.exists():
+        return None
+    r = np.load(ref_path)
+    ref = r["mean"].astype(np.float64)
+    res = int(r["width"])
+    s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
+    par = dict(par, width=res, height=res)
+    sc = are.Scene(s)
+    gp = are.GuideParams.make(batch=1 << 16)
+
+    def relmse(img):
+        return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+    def timed(fn):
+        t = time.perf_counter()
+        out = fn()
+        return out, time.perf_counter() - t
+
+    # calibrate seconds per sample of each method
+    _, tg = timed(lambda: sc.render_guided(are.Guide(seed=90), cam, dict(par, spp=256, seed=90), gp, with_var=False))
+    _, tp = timed(lambda: sc.render(cam, dict(par, spp=256, seed=91), with_var=False))
+    spp_g = max(1, int(budget_s / (tg / 256)))
+    spp_p = max(1, int(budget_s / (tp / 256)))
+    (gi, _, gst), t_g = timed(lambda: sc.render_guided(are.Guide(seed=1), cam, dict(par, spp=spp_g, seed=1), gp,
+                                                       with_var=False))
+    (pi, _, _), t_p = timed(lambda: sc.render(cam, dict(par, spp=spp_p, seed=2), with_var=False))
+    eg, ep = relmse(gi), relmse(pi)
+    sc.close()
+    return {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]),
+            "budget_s": budget_s,
+            "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)},
+            "guided": {"spp": spp_g, "seconds": round(t_g, 3), "relmse": round(eg, 6),
+                       "adam_steps": gst["train_steps"]},
+            "relmse_plain_over_guided": round(ep / eg, 3)}
+
+
 def run_reference(args, rank, world) -> None:
     """--impl reference: the CPU implementation of the path on the host cores."""
     if rank != 0:
@@ -183,6 +230,7 @@ def main() -> None:
     ap.add_argument("--pool", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-guiding", action="store_true", help="skip the guided-vs-plain relMSE comparison")
     ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -284,6 +332,10 @@ def main() -> None:
     e2e = {"value": round(samples_per_step / statistics.median(e2e_times) / 1e6 * world, 3), "unit": UNIT,
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.nbytes)}
 
+    guiding = None
+    if rank == 0 and args.workload == "cornell" and not args.no_guiding:
+        guiding = guiding_eval()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -304,7 +356,7 @@ def main() -> None:
             "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
             "wall_s": round(wall, 3),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "clocks": clk.summary(), "gpu_launches": gpu_launches,
+            "clocks": clk.summary(), "gpu_launches": gpu_launches, "guiding_equal_time": guiding,
         }
         print(json.dumps(line), flush=True)
     sc.close()

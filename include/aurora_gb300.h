@@ -163,6 +163,7 @@ typedef struct are_render_stats {
 	int64_t kernel_launches[4]; /* launches per kernel kind */
 	int32_t error_word;         /* device error bits, 0 = clean */
 	int32_t reserved_;
+	double aux[4];              /* are_render_guided: training samples, Adam steps, guided vertices, last loss */
 } are_render_stats;
 
 /* ---- entry points ------------------------------------------------------- */
@@ -231,9 +232,82 @@ ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n,
  * events are created. */
 #define ARE_NOALLOC_MAX_PATHS 65536
 #define ARE_NOALLOC_MAX_PIXELS 524288
-#define ARE_NOALLOC_SCRATCH_BYTES (28u * 1024u * 1024u)
+#define ARE_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 ARE_API are_status are_render_noalloc(are_scene *scene, const are_camera *camera, const are_render_params *params,
 	float *rgb_out, float *var_out, are_render_stats *stats);
+
+/* ---- path guiding ------------------------------------------------------- */
+
+/* No counterpart in the reference (it has no guiding).  A small network
+ * (12-frequency encoding of position, normal and outgoing direction; four
+ * 64-wide ReLU layers; 8 von Mises-Fisher lobes) that learns where incident
+ * radiance comes from, trained online from the renderer's own samples with
+ * Adam.  FP16 tensor-core arithmetic, FP32 accumulation and master weights.
+ * Parameter layout and loss: oracle/orc_guide.c. */
+typedef struct are_guide are_guide;
+ARE_API int32_t are_guide_param_count(void);
+ARE_API are_status are_guide_create(uint64_t seed, are_guide **out);
+ARE_API are_status are_guide_destroy(are_guide *guide);
+ARE_API are_status are_guide_get_params(are_guide *guide, float *params_out);
+ARE_API are_status are_guide_set_params(are_guide *guide, const float *params);  /* also resets Adam */
+/* raw network outputs (n x 48, host) for features (n x 9, host) */
+ARE_API are_status are_guide_forward(are_guide *guide, const float *features, int64_t n, float *out);
+/* samples: n x 13 host floats (features 9, direction 3, weight 1).  Mean loss
+ * and its gradient (are_guide_param_count() floats), parameters unchanged. */
+ARE_API are_status are_guide_gradient(are_guide *guide, const float *samples, int64_t n, float *loss, float *grad);
+/* losses of the most recent Adam steps taken inside renders (oldest first);
+ * returns how many were written (at most max) */
+ARE_API int32_t are_guide_loss_history(are_guide *guide, float *out, int32_t max);
+/* one Adam step (beta1 0.9, beta2 0.99) on a batch; loss before the step */
+ARE_API are_status are_guide_train(are_guide *guide, const float *samples, int64_t n, float lr, float *loss);
+
+typedef struct are_guide_params {
+	float mix;            /* probability of drawing a guided vertex's direction from the network (one-sample MIS) */
+	int32_t guide_depth;  /* diffuse bounces guided per path: 0 .. 4 */
+	int32_t train;        /* train the network online during the render */
+	int32_t batch;        /* training samples per Adam step (e.g. 2^18) */
+	float lr;             /* Adam learning rate */
+	float weight_clip;    /* cap on a sample's weight relative to the batch mean (0 = none) */
+	int32_t reserved_[2];
+} are_guide_params;
+
+/* The path estimator (ARE_EST_PATH) with guided diffuse bounces: at each of
+ * the first guide_depth diffuse vertices the direction is drawn from the
+ * network's mixture with probability mix, else by cosine sampling, and
+ * weighted by the combined density, so the image stays unbiased whatever the
+ * network has learned.  With train != 0 the network trains on the render's
+ * own paths (stats->reserved_ returns the number of Adam steps taken). */
+ARE_API are_status are_render_guided(are_scene *scene, are_guide *guide, const are_camera *camera,
+	const are_render_params *params, const are_guide_params *guide_params, float *rgb_out, float *var_out,
+	are_render_stats *stats);
+
+/* ---- many scenes in one launch ------------------------------------------ */
+
+/* Launch shape of are_render_batch; 0 fields take defaults (256 threads, 4). */
+typedef struct are_batch_options {
+	int32_t block_size;   /* threads per block of the persistent kernel */
+	int32_t fetch;        /* work items per lane taken with each atomic on the shared queue */
+	int32_t leaf_size;    /* BVH leaf size the scenes were built with (reported by the autotuner) */
+	int32_t reserved_;
+} are_batch_options;
+
+/* No counterpart in the reference (it renders one scene).  Renders n scenes of
+ * any size, resolution and spp in one persistent kernel launch over a shared
+ * work queue (pixel x sample-chunk items of all scenes), captured with its
+ * clears and resolves in one CUDA graph.  Same path estimator and random
+ * numbers as are_render with ARE_EST_PATH; per-pixel sums use FP32 atomics.
+ * rgb_out[i] (host, may be NULL to skip) receives scene i's mean radiance;
+ * scene_ms[i] (may be NULL) its completion time from the start of the launch.
+ * All scenes must live on one device. */
+ARE_API are_status are_render_batch(are_scene *const *scenes, const are_camera *cameras,
+	const are_render_params *params, int32_t n, const are_batch_options *options, float *const *rgb_out,
+	double *scene_ms, are_render_stats *stats);
+
+/* Times the batch on a calibration run (spp capped at calib_spp) for every
+ * BVH leaf size {2,4,8} x block size {128,256,512} x fetch {1,4,16}, building
+ * the scenes from their descriptors, and returns the fastest combination. */
+ARE_API are_status are_batch_autotune(const are_scene_desc *const *descs, const are_camera *cameras,
+	const are_render_params *params, int32_t n, int32_t calib_spp, are_batch_options *best, double *best_ms);
 
 /* ---- synthetic workloads ------------------------------------------------ */
 
@@ -242,7 +316,11 @@ enum {
 	ARE_CONFIG_CORNELL = 1,         /* 19 quads, 600x600, 1024 spp, depth 50 */
 	ARE_CONFIG_MESH = 2,            /* displaced icosphere, 1920x1080, 256 spp, depth 16 */
 	ARE_CONFIG_CORNELL_OCCLUDED = 4,/* Cornell + occluder under the light, depth 16 */
-	ARE_CONFIG_LEGACY_RT = 5        /* rt.cpp's own 34-triangle scene (rt.cpp:153-167) */
+	ARE_CONFIG_LEGACY_RT = 5,       /* rt.cpp's own 34-triangle scene (rt.cpp:153-167) */
+	ARE_CONFIG_SPHERE_FIELD = 6     /* one scene of the uneven batch: mesh_frequency = sphere count
+	                                   (>= 1) on a jittered grid, materials as RANDOM_SPHERES; the
+	                                   resolution (256x256, 640x360, 1280x720) and spp (16, 64, 256)
+	                                   are drawn from the seed */
 };
 
 typedef struct are_config are_config; /* owns the arrays its descriptor points at */

@@ -20,7 +20,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-ORACLE_SOURCES = ["orc_common.c", "orc_f32.c", "orc_f64.c", "orc_legacy.c"]
+ORACLE_SOURCES = ["orc_common.c", "orc_f32.c", "orc_f64.c", "orc_legacy.c", "orc_guide.c"]
 REF_LIB_SOURCES = [
     "src/basic/vec3.cpp",
     "src/basic/ray.cpp",

@@ -142,6 +142,14 @@ void orc_ppm_quantize(const float *rgb, int64_t n, float gamma, uint8_t *out); /
  * counter-based per pixel keyed by p->seed.  rgb: width*height*3. */
 int32_t orc_render_legacy(const orc_ctx *ctx, const orc_camera *cam, const orc_params *p, float *rgb, int32_t rng_mode,
 	uint32_t mt_seed, int32_t nthreads);
+/* Path-guiding network in FP64 (orc_guide.c): parameters are one flat float array. */
+int32_t orc_guide_num_params(void);
+void orc_guide_encode(const double *x, double *e);
+void orc_guide_forward(const float *params, const float *feat, int64_t n, double *out);
+double orc_guide_pdf(const double *o48, const double *w);
+double orc_guide_loss_grad(const float *params, const float *samples, int64_t n, double *grad);
+void orc_guide_adam(float *params, float *m, float *v, const double *grad, int64_t step, double lr, double b1, double b2,
+	double eps);
 /* std::mt19937(seed): n raw outputs and n uniform_real_distribution<float>(0,1) draws */
 void orc_mt19937(uint32_t seed, int64_t n, uint32_t *out, float *canon);
 

@@ -152,7 +152,35 @@ class Oracle:
         L.orc_render_legacy.argtypes = [C.c_void_p, C.POINTER(OrcCamera), C.POINTER(OrcParams), _f, C.c_int32,
                                         C.c_uint32, C.c_int32]
         L.orc_mt19937.argtypes = [C.c_uint32, C.c_int64, C.POINTER(C.c_uint32), _f]
+        L.orc_guide_num_params.restype = C.c_int32
+        L.orc_guide_forward.argtypes = [_f, _f, C.c_int64, _d]
+        L.orc_guide_pdf.restype = C.c_double
+        L.orc_guide_pdf.argtypes = [_d, _d]
+        L.orc_guide_loss_grad.restype = C.c_double
+        L.orc_guide_loss_grad.argtypes = [_f, _f, C.c_int64, _d]
+        L.orc_guide_encode.argtypes = [_d, _d]
         self.lib = L
+
+    # path-guiding network (FP64) -------------------------------------------------
+    def guide_forward(self, params: np.ndarray, feat: np.ndarray) -> np.ndarray:
+        params = np.ascontiguousarray(params, np.float32)
+        feat = np.ascontiguousarray(feat, np.float32).reshape(-1, 9)
+        out = np.zeros((len(feat), 48))
+        self.lib.orc_guide_forward(_ptr(params, _f), _ptr(feat.reshape(-1), _f), len(feat), _ptr(out.reshape(-1), _d))
+        return out
+
+    def guide_loss_grad(self, params: np.ndarray, samples: np.ndarray):
+        params = np.ascontiguousarray(params, np.float32)
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
+        grad = np.zeros(self.lib.orc_guide_num_params())
+        loss = self.lib.orc_guide_loss_grad(_ptr(params, _f), _ptr(samples.reshape(-1), _f), len(samples),
+                                            _ptr(grad, _d))
+        return loss, grad
+
+    def guide_pdf(self, out48: np.ndarray, w: np.ndarray) -> float:
+        o = np.ascontiguousarray(out48, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        return self.lib.orc_guide_pdf(_ptr(o, _d), _ptr(w, _d))
 
     class Ctx:
         def __init__(self, orc, scene, accel):

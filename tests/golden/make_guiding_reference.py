@@ -1,0 +1,67 @@
+"""FP64 CPU reference of the occluded-light Cornell box (guiding evaluation).
+
+The oracle's FP64 path estimator (oracle/orc_f64.c) renders the occluded
+Cornell workload (600x600 in the workload definition; 200x200 here, same
+camera, so the FP64 CPU render finishes in minutes rather than hours) at
+65,536 samples per pixel, depth 16, Russian roulette from depth 3, as 64
+independent 1,024-spp passes with different seeds.  The mean image and its
+per-pixel variance of the mean are saved as float32 to
+tests/golden/guiding_reference_200.npz; partial progress is kept in
+baseline/_ref/ so an interrupted run resumes.
+
+Usage: python tests/golden/make_guiding_reference.py [passes] [threads]
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "tests"))
+
+from common import are  # noqa: E402
+from oracle.orc import Oracle  # noqa: E402
+
+RES = 200
+PASS_SPP = 1024
+
+
+def main() -> None:
+    passes = int(sys.argv[1]) if len(sys.argv) > 1 else 64
+    threads = int(sys.argv[2]) if len(sys.argv) > 2 else (os.cpu_count() or 1)
+    part = REPO / "baseline" / "_ref" / "guiding_reference_partial.npz"
+    part.parent.mkdir(parents=True, exist_ok=True)
+    s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
+    par = dict(par, width=RES, height=RES, spp=PASS_SPP)
+    orc = Oracle()
+    ctx = orc.prepare(s)
+    done, s1, s2 = 0, np.zeros((RES, RES, 3)), np.zeros((RES, RES, 3))
+    if part.exists():
+        z = np.load(part)
+        done, s1, s2 = int(z["done"]), z["s1"], z["s2"]
+    while done < passes:
+        t = time.time()
+        m, v, st = orc.render(ctx, cam, dict(par, seed=100_000 + done), fp64=True, nthreads=threads)
+        # per pass: mean m and variance of its mean v; combine passes exactly
+        s1 += m
+        s2 += v * PASS_SPP * (PASS_SPP - 1) + PASS_SPP * m * m  # sum of squares of the pass's samples
+        done += 1
+        np.savez(part, done=done, s1=s1, s2=s2)
+        print(f"pass {done}/{passes} {time.time() - t:.1f}s", flush=True)
+    n = done * PASS_SPP
+    mean = s1 / done
+    var = (s2 - n * mean * mean) / (n - 1) / n
+    np.savez_compressed(HERE / "guiding_reference_200.npz", mean=mean.astype(np.float32),
+                        var=np.maximum(var, 0).astype(np.float32), spp=n, width=RES, height=RES,
+                        config=are.CONFIG_CORNELL_OCCLUDED)
+    print("saved", n, "spp")
+
+
+if __name__ == "__main__":
+    main()

@@ -130,3 +130,24 @@ def test_mesh_triangle_count_and_watertight_edges():
             keys[e] = keys.get(e, 0) + 1
     assert set(keys.values()) == {2}
     assert s.triangle_test == are.TRI_WATERTIGHT
+
+
+def test_ctypes_structs_match_the_header():
+    """Every C struct of include/aurora_gb300.h has the size its ctypes mirror
+    assumes (a mismatch lets the library write past the Python object)."""
+    import subprocess
+    import tempfile
+    from pathlib import Path
+    structs = {"are_material": are.MATERIAL_DTYPE.itemsize, "are_texture": are.TEXTURE_DTYPE.itemsize,
+               "are_scene_desc": C.sizeof(are.SceneDesc), "are_camera": C.sizeof(are.Camera),
+               "are_render_params": C.sizeof(are.RenderParams), "are_render_stats": C.sizeof(are.RenderStats),
+               "are_guide_params": C.sizeof(are.GuideParams), "are_batch_options": C.sizeof(are.BatchOptions)}
+    src = '#include "aurora_gb300.h"\n#include <stdio.h>\nint main(void){\n' + "".join(
+        f'printf("%zu\\n", sizeof({k}));\n' for k in structs) + "return 0;}\n"
+    with tempfile.TemporaryDirectory() as td:
+        c = Path(td) / "s.c"
+        c.write_text(src)
+        exe = Path(td) / "s"
+        subprocess.run(["gcc", "-I", str(REPO / "include"), str(c), "-o", str(exe)], check=True)
+        sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert dict(zip(structs, sizes)) == structs

@@ -1,0 +1,58 @@
+"""Many uneven scenes in one persistent launch (are_render_batch): each
+scene's image agrees with the wavefront renderer's (same estimator, same
+random numbers), every scene completes, and the autotuner returns a valid
+launch shape."""
+import numpy as np
+import pytest
+
+from common import are
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(n=6):
+    wl = are.batch_workload(n_scenes=n, seed=7, min_count=50, max_count=20000)
+    scenes, cams, params, arrays = [], [], [], []
+    for i, (s, cam, par) in enumerate(wl):
+        par = dict(par, width=min(par["width"], 96), height=min(par["height"], 64), spp=16 + 8 * (i % 3), seed=100 + i)
+        arrays.append(s)
+        scenes.append(are.Scene(s))
+        cams.append(cam)
+        params.append(par)
+    return arrays, scenes, cams, params
+
+
+def test_batch_matches_wavefront_per_scene(gpu_lib):
+    arrays, scenes, cams, params = small_batch()
+    imgs, ms, st = are.render_batch(scenes, cams, params)
+    assert st["error_word"] == 0 and st["samples"] == sum(p["width"] * p["height"] * p["spp"] for p in params)
+    assert all(m > 0 for m in ms)
+    for img, sc, cam, par in zip(imgs, scenes, cams, params):
+        ref, var, _ = sc.render(cam, par)
+        assert np.isfinite(img).all()
+        # same random numbers: per-pixel agreement to float rounding except rare path divergence
+        close = np.abs(img - ref) <= 1e-4 * np.maximum(1.0, np.abs(ref))
+        assert close.mean() > 0.95, close.mean()
+        assert abs(img.mean() - ref.mean()) < 1e-3 * max(1.0, ref.mean())
+
+
+def test_batch_launch_shapes_agree(gpu_lib):
+    arrays, scenes, cams, params = small_batch(4)
+    a, _, _ = are.render_batch(scenes, cams, params, are.BatchOptions(128, 1, 0, 0))
+    b, _, _ = are.render_batch(scenes, cams, params, are.BatchOptions(512, 16, 0, 0))
+    for x, y in zip(a, b):
+        # FP32 atomics add the chunks in a different order: equal to rounding
+        assert np.allclose(x, y, rtol=1e-5, atol=1e-6)
+
+
+def test_autotune_returns_a_valid_shape(gpu_lib):
+    arrays, scenes, cams, params = small_batch(3)
+    best, ms = are.batch_autotune(arrays, cams, params, calib_spp=1)
+    assert best.block_size in (128, 256, 512) and best.fetch in (1, 4, 16) and best.leaf_size in (2, 4, 8)
+    assert ms > 0
+
+
+def test_batch_rejects_bad_options(gpu_lib):
+    arrays, scenes, cams, params = small_batch(2)
+    with pytest.raises(are.AreError):
+        are.render_batch(scenes, cams, params, are.BatchOptions(100, 1, 0, 0))

@@ -1,0 +1,84 @@
+"""Guided rendering (are_render_guided) on the occluded-light Cornell box:
+unbiased against the plain estimator, and its error against the FP64 CPU
+reference (tests/golden/guiding_reference_200.npz, 65,536 spp) at equal
+samples and at equal time."""
+import time
+
+import numpy as np
+import pytest
+
+from common import GOLDEN, are
+
+pytestmark = pytest.mark.gpu
+REF = GOLDEN / "guiding_reference_200.npz"
+
+
+def rel_mse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def c4(res, spp, **kw):
+    s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
+    return s, cam, dict(par, width=res, height=res, spp=spp, **kw)
+
+
+def test_guided_is_unbiased(gpu_lib):
+    s, cam, par = c4(48, 2048, seed=3)
+    sc = are.Scene(s)
+    g = are.Guide(seed=5)
+    img, var, st = sc.render_guided(g, cam, par, are.GuideParams.make(batch=1 << 16))
+    ref, rvar, _ = sc.render(cam, dict(par, spp=8192, seed=4))
+    assert st["train_steps"] > 0 and st["error_word"] == 0
+    assert np.isfinite(img).all()
+    z = np.abs(img - ref) / np.sqrt(var + rvar + 1e-12)
+    assert (z > 3).mean() < 0.02, (z > 3).mean()
+    # image means agree within their standard errors
+    se = np.sqrt(var.sum() + rvar.sum()) / img.size
+    assert abs(img.mean() - ref.mean()) < 5 * se + 1e-5
+
+
+@pytest.mark.skipif(not REF.exists(), reason="FP64 reference not generated")
+def test_guided_beats_plain_at_equal_samples(gpu_lib):
+    r = np.load(REF)
+    ref = r["mean"].astype(np.float64)
+    res = int(r["width"])
+    s, cam, par = c4(res, 256, seed=7)
+    sc = are.Scene(s)
+    g = are.Guide(seed=1)
+    # warm the network on one render, then measure a fresh render with the trained network
+    sc.render_guided(g, cam, dict(par, seed=100), are.GuideParams.make(batch=1 << 16))
+    gi, _, st = sc.render_guided(g, cam, par, are.GuideParams.make(batch=1 << 16))
+    pi, _, _ = sc.render(cam, par)
+    e_g, e_p = rel_mse(gi, ref), rel_mse(pi, ref)
+    print(f"equal spp (256): relMSE guided {e_g:.4g} plain {e_p:.4g} ratio {e_p / e_g:.2f}")
+    assert e_g < e_p
+
+
+@pytest.mark.skipif(not REF.exists(), reason="FP64 reference not generated")
+def test_guided_vs_plain_at_equal_time(gpu_lib):
+    r = np.load(REF)
+    ref = r["mean"].astype(np.float64)
+    res = int(r["width"])
+    s, cam, par = c4(res, 64, seed=9)
+    sc = are.Scene(s)
+    # time per sample of each method (training included for the guided one)
+    g = are.Guide(seed=2)
+    t = time.perf_counter()
+    sc.render_guided(g, cam, dict(par, spp=512), are.GuideParams.make(batch=1 << 16))
+    tg = (time.perf_counter() - t) / 512
+    t = time.perf_counter()
+    sc.render(cam, dict(par, spp=512), with_var=False)
+    tp = (time.perf_counter() - t) / 512
+    budget = 0.1  # seconds per render
+    spp_g, spp_p = max(1, int(budget / tg)), max(1, int(budget / tp))
+    g2 = are.Guide(seed=3)
+    t = time.perf_counter()
+    gi, _, st = sc.render_guided(g2, cam, dict(par, spp=spp_g, seed=11), are.GuideParams.make(batch=1 << 16))
+    tgr = time.perf_counter() - t
+    t = time.perf_counter()
+    pi, _, _ = sc.render(cam, dict(par, spp=spp_p, seed=12))
+    tpr = time.perf_counter() - t
+    e_g, e_p = rel_mse(gi, ref), rel_mse(pi, ref)
+    print(f"equal time: guided {spp_g} spp {tgr:.3f}s relMSE {e_g:.4g}; plain {spp_p} spp {tpr:.3f}s relMSE {e_p:.4g}; "
+          f"ratio {e_p / e_g:.2f}; train steps {st['train_steps']}")
+    assert e_g <= e_p * 1.25  # guiding must not lose at equal time
