@@ -32,6 +32,7 @@ EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
 FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
 CONFIG_SPHERE_FIELD = 6
+TONEMAP_GAMMA, TONEMAP_LINEAR = 0, 1
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("texture", "<i4"), ("fuzz", "<f4"), ("ior", "<f4"),
                            ("emit", "<f4", 3), ("reflect_ratio", "<f4"), ("tint", "<f4", 3), ("pad_", "<f4")])
@@ -41,7 +42,7 @@ TEXTURE_DTYPE = np.dtype([("type", "<i4"), ("mapping", "<i4"), ("scale", "<f4"),
 assert MATERIAL_DTYPE.itemsize == 48 and TEXTURE_DTYPE.itemsize == 64
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "no device",
-          5: "kernel timeout", 6: "internal error"}
+          5: "kernel timeout", 6: "internal error", 7: "file error"}
 
 
 class AreError(RuntimeError):
@@ -185,6 +186,10 @@ class BatchOptions(C.Structure):
         return {"block_size": self.block_size, "fetch": self.fetch, "leaf_size": self.leaf_size}
 
 
+class TonemapParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("gamma", C.c_float), ("flags", C.c_uint32), ("reserved_", C.c_int32)]
+
+
 class GuideParams(C.Structure):
     _fields_ = [("mix", C.c_float), ("guide_depth", C.c_int32), ("train", C.c_int32), ("batch", C.c_int32),
                 ("lr", C.c_float), ("weight_clip", C.c_float), ("reserved_", C.c_int32 * 2)]
@@ -324,6 +329,10 @@ def load(path: str | os.PathLike | None = None):
                                    C.POINTER(RenderStats)]
     L.are_batch_autotune.argtypes = [C.POINTER(C.POINTER(SceneDesc)), C.POINTER(Camera), C.POINTER(RenderParams),
                                      C.c_int32, C.c_int32, C.POINTER(BatchOptions), C.POINTER(C.c_double)]
+    L.are_tonemap.argtypes = [C.c_void_p, C.c_int64, C.POINTER(TonemapParams), C.c_void_p]
+    L.are_write_ppm.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]
+    L.are_write_pfm.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]
+    L.are_read_ppm.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p]
     L.are_guide_loss_history.restype = C.c_int32
     L.are_guide_loss_history.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
     L.are_guide_param_count.restype = C.c_int32
@@ -332,6 +341,7 @@ def load(path: str | os.PathLike | None = None):
     L.are_guide_get_params.argtypes = [C.c_void_p, C.c_void_p]
     L.are_guide_set_params.argtypes = [C.c_void_p, C.c_void_p]
     L.are_guide_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    L.are_guide_mixture.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.are_guide_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p]
     L.are_guide_train.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.POINTER(C.c_float)]
     for name in exported_symbols():
@@ -491,6 +501,13 @@ class Guide:
         check(self.lib.are_guide_forward(self.h, feat.ctypes.data, len(feat), out.ctypes.data))
         return out
 
+    def mixture(self, feat: np.ndarray) -> np.ndarray:
+        """are_guide_mixture: the packed vMF mixture per row (n x 48)."""
+        feat = np.ascontiguousarray(feat, np.float32).reshape(-1, 9)
+        out = np.empty((len(feat), 48), np.float32)
+        check(self.lib.are_guide_mixture(self.h, feat.ctypes.data, len(feat), out.ctypes.data))
+        return out
+
     def gradient(self, samples: np.ndarray):
         samples = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)
         g = np.empty(self.n_params, np.float32)
@@ -550,4 +567,47 @@ def batch_workload(n_scenes: int = 64, seed: int = 2026, min_count: int = 50, ma
     for i in range(n_scenes):
         cnt = int(np.exp(rng.uniform(np.log(min_count), np.log(max_count))))
         out.append(build_config(CONFIG_SPHERE_FIELD, seed=seed * 1000 + i, mesh_frequency=cnt))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# output formats
+
+
+def tonemap(rgb: np.ndarray, mode: int = TONEMAP_GAMMA, gamma: float = 2.2) -> np.ndarray:
+    """are_tonemap of a host float32 image (any shape) -> uint8 of the same shape."""
+    L = load()
+    a = np.ascontiguousarray(rgb, np.float32)
+    out = np.empty(a.shape, np.uint8)
+    check(L.are_tonemap(a.ctypes.data, a.size, C.byref(TonemapParams(mode, gamma, 0, 0)), out.ctypes.data))
+    return out
+
+
+def tonemap_device(rgb_ptr: int, n_values: int, out_ptr: int, mode: int = TONEMAP_GAMMA, gamma: float = 2.2) -> None:
+    """are_tonemap on device pointers of the current device."""
+    L = load()
+    check(L.are_tonemap(rgb_ptr, n_values, C.byref(TonemapParams(mode, gamma, FLAG_DEVICE_OUTPUT, 0)), out_ptr))
+
+
+def write_ppm(path, rgb8: np.ndarray) -> None:
+    """are_write_ppm of an (h, w, 3) uint8 image."""
+    a = np.ascontiguousarray(rgb8, np.uint8)
+    h, w = a.shape[:2]
+    check(load().are_write_ppm(os.fsencode(path), a.ctypes.data, w, h))
+
+
+def write_pfm(path, rgb: np.ndarray) -> None:
+    """are_write_pfm of an (h, w, 3) float32 image."""
+    a = np.ascontiguousarray(rgb, np.float32)
+    h, w = a.shape[:2]
+    check(load().are_write_pfm(os.fsencode(path), a.ctypes.data, w, h))
+
+
+def read_ppm(path) -> np.ndarray:
+    """are_read_ppm -> (h, w, 3) float32 texels, byte / 255."""
+    L = load()
+    w, h = C.c_int32(), C.c_int32()
+    check(L.are_read_ppm(os.fsencode(path), C.byref(w), C.byref(h), None))
+    out = np.empty((h.value, w.value, 3), np.float32)
+    check(L.are_read_ppm(os.fsencode(path), C.byref(w), C.byref(h), out.ctypes.data))
     return out

@@ -20,6 +20,8 @@ REPO = HERE.parent
 CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "libaurora_gb300.so"
+CLI_SRC = HERE / "cli" / "are_render.cpp"
+CLI = OUT / "are_render"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -72,7 +74,21 @@ def build(force: bool = False, jobs: int | None = None) -> Path:
         _run([nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs), "-lpthread", "-ldl",
               "-lrt"])
         os.replace(tmp, LIB)
+    build_cli(force)
     return LIB
+
+
+def build_cli(force: bool = False) -> Path:
+    """The command-line renderer, a C++ program over include/aurora_gb300.hpp
+    linked against the library (found next to it at run time)."""
+    deps = [CLI_SRC, LIB, REPO / "include" / "aurora_gb300.hpp", REPO / "include" / "aurora_gb300.h"]
+    if force or not CLI.exists() or CLI.stat().st_mtime < max(d.stat().st_mtime for d in deps):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        tmp = CLI.with_name(CLI.name + ".tmp%d" % os.getpid())
+        _run([cxx, "-O2", "-std=c++17", "-Wall", "-I", str(REPO / "include"), str(CLI_SRC), "-o", str(tmp),
+              "-L", str(OUT), "-laurora_gb300", "-Wl,-rpath,$ORIGIN"])
+        os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

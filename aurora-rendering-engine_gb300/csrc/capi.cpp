@@ -45,6 +45,7 @@ ARE_API const char *are_status_string(are_status s) {
 	case ARE_ERR_NO_DEVICE: return "no device";
 	case ARE_ERR_KERNEL_TIMEOUT: return "kernel timeout";
 	case ARE_ERR_INTERNAL: return "internal error";
+	case ARE_ERR_IO: return "file error";
 	}
 	return "unknown status";
 }
@@ -110,6 +111,22 @@ ARE_API are_status are_batch_autotune(const are_scene_desc *const *descs, const 
 ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n, float *hits, int32_t device_ptrs,
 	float *ms_out) {
 	return guarded([&] { return are_core::intersect(scene, rays, n, hits, device_ptrs, ms_out); });
+}
+
+ARE_API are_status are_tonemap(const float *rgb, int64_t n_values, const are_tonemap_params *params, uint8_t *out) {
+	return guarded([&] { return are_core::tonemap(rgb, n_values, params, out); });
+}
+
+ARE_API are_status are_write_ppm(const char *path, const uint8_t *rgb8, int32_t width, int32_t height) {
+	return guarded([&] { return are_core::write_ppm(path, rgb8, width, height); });
+}
+
+ARE_API are_status are_write_pfm(const char *path, const float *rgb, int32_t width, int32_t height) {
+	return guarded([&] { return are_core::write_pfm(path, rgb, width, height); });
+}
+
+ARE_API are_status are_read_ppm(const char *path, int32_t *width, int32_t *height, float *texels) {
+	return guarded([&] { return are_core::read_ppm(path, width, height, texels); });
 }
 
 ARE_API are_status are_config_build(int32_t config, uint64_t seed, int32_t mesh_frequency, are_config **out) {

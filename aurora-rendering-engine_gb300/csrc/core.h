@@ -39,6 +39,7 @@ enum : uint32_t {
 	ERR_QUEUE_OVERFLOW = 2u,
 	ERR_BAD_INDEX = 4u,
 	ERR_NONFINITE = 8u,
+	ERR_TENSOR_TIMEOUT = 16u,  // a bounded wait for tensor-core work or a bulk copy gave up
 };
 
 struct DevMaterial {  // mirrors are_material (48 B)

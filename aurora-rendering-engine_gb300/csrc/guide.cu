@@ -3,7 +3,9 @@
 //
 //   k_guide_pack    FP32 master parameters -> FP16 weight image (forward rows
 //                   and transposed rows for the backward pass) + FP32 biases
-//   k_guide_infer   fused forward of 16-row tiles on the tensor cores
+//   k_guide_pack_tc FP32 master parameters -> the tcgen05 weight image
+//   k_guide_infer   fused forward of 128-row tiles on the 5th-generation
+//                   tensor cores (tcgen05.mma, accumulators in tensor memory)
 //   k_guide_fwdbwd  fused forward + loss gradient + backward per 16-sample
 //                   tile; stores each layer's input and output gradient (FP16)
 //   k_guide_wgrad   weight gradients dW = sum_s delta_s h_s^T on the tensor
@@ -21,6 +23,7 @@
 #include "guide.cuh"
 #include "guide_host.h"
 #include "scene.h"
+#include "tc05.cuh"
 
 namespace are_core {
 
@@ -61,6 +64,26 @@ __global__ void k_guide_pack(const float *__restrict__ P, __half *__restrict__ i
 	}
 }
 
+__global__ void k_guide_pack_tc(const float *__restrict__ P, __half *__restrict__ img) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < TC_HALVES; i += gridDim.x * blockDim.x) {
+		// invert tc_index for the layer holding i
+		int base, K, off, boff, rows_used;
+		if (i < TC_W2) base = TC_W1, K = TC_K1, off = OFF_W1, boff = OFF_B1, rows_used = GN_H;
+		else if (i < TC_W3) base = TC_W2, K = TC_KH, off = OFF_W2, boff = OFF_B2, rows_used = GN_H;
+		else if (i < TC_W4) base = TC_W3, K = TC_KH, off = OFF_W3, boff = OFF_B3, rows_used = GN_H;
+		else if (i < TC_W5) base = TC_W4, K = TC_KH, off = OFF_W4, boff = OFF_B4, rows_used = GN_H;
+		else base = TC_W5, K = TC_KH, off = OFF_W5, boff = OFF_B5, rows_used = 40;
+		const int j = i - base, grp = j / (K * 8), rem = j - grp * (K * 8);
+		const int kc = rem >> 6, in = rem & 63;
+		const int row = grp * 8 + (in >> 3), k = kc * 8 + (in & 7);
+		const int in_cols = base == TC_W1 ? GN_ENC : GN_H;   // columns of the FP32 matrix
+		const int one = base == TC_W1 ? TC_ONE1 : GN_H;       // the bias column
+		float v = 0.0f;
+		if (row < rows_used) v = k == one ? P[boff + row] : (k < one ? P[off + row * in_cols + k] : 0.0f);
+		img[i] = __float2half_rn(v);
+	}
+}
+
 // Copies `halves` halves and IMG_BIAS floats of the image into shared memory.
 __device__ __forceinline__ void load_image(const __half *img, const float *bias, int halves, __half *s_img,
 	float *s_bias) {
@@ -81,18 +104,22 @@ __device__ __forceinline__ void tile_forward(const __half *s_img, const float *s
 #pragma unroll
 	for (int nt = 0; nt < 8; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
 	const int g = (threadIdx.x & 31) >> 2;
+	// running (sin, cos) of the feature being encoded, rows g and g+8
+	float s0 = 0.f, k0 = 1.f, s1 = 0.f, k1 = 1.f;
+#pragma unroll
 	for (int ks = 0; ks < GN_ENC / 16; ++ks) {
 		uint32_t a[4];
-		a[0] = h2u(enc_pair(x0, ks * 8 + t));
-		a[1] = h2u(enc_pair(x1, ks * 8 + t));
-		a[2] = h2u(enc_pair(x0, ks * 8 + 4 + t));
-		a[3] = h2u(enc_pair(x1, ks * 8 + 4 + t));
+		a[0] = h2u(enc_quad(x0, ks * 8, t, s0, k0));
+		a[1] = h2u(enc_quad(x1, ks * 8, t, s1, k1));
+		a[2] = h2u(enc_quad(x0, ks * 8 + 4, t, s0, k0));
+		a[3] = h2u(enc_quad(x1, ks * 8 + 4, t, s1, k1));
 		if (h0_out0) {
 			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 2 * t) = a[0];
 			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 2 * t) = a[1];
 			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 8 + 2 * t) = a[2];
 			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 8 + 2 * t) = a[3];
 		}
+		if (ks * 8 >= 116) continue;  // pairs 116.. of the encoding are zero
 #pragma unroll
 		for (int nt = 0; nt < 8; ++nt) {
 			const __half *row = s_img + IMG_W1 + (nt * 8 + g) * S_ENC + ks * 16 + 2 * t;
@@ -119,30 +146,255 @@ __device__ __forceinline__ void tile_forward(const __half *s_img, const float *s
 	}
 }
 
-__global__ void __launch_bounds__(GT) k_guide_infer(const __half *__restrict__ img, const float *__restrict__ bias,
-	const float *__restrict__ feat, int n, const unsigned *__restrict__ n_dev, float *__restrict__ out) {
-	if (n_dev) n = min(n, (int)*n_dev);
-	extern __shared__ __align__(16) unsigned char smem[];
-	__half *s_img = reinterpret_cast<__half *>(smem);
-	float *s_bias = reinterpret_cast<float *>(smem + IMG_FWD * sizeof(__half));
-	load_image(img, bias, IMG_FWD, s_img, s_bias);
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	const int tiles = (n + 15) / 16;
-	for (int tile = blockIdx.x * (GT / 32) + warp; tile < tiles; tile += gridDim.x * (GT / 32)) {
-		int r0 = tile * 16 + g, r1 = r0 + 8;
-		float x0[GN_IN], x1[GN_IN];
-		for (int k = 0; k < GN_IN; ++k) {
-			x0[k] = r0 < n ? feat[(size_t)r0 * GN_IN + k] : 0.f;
-			x1[k] = r1 < n ? feat[(size_t)r1 * GN_IN + k] : 0.f;
-		}
-		float c5[6][4];
-		tile_forward(s_img, s_bias, x0, x1, c5, nullptr, nullptr, nullptr);
+// ---- inference on the 5th-generation tensor cores ---------------------------
+//
+// A block is four warpgroups; each warpgroup runs 128-row tiles on its own
+// (thread t of the warpgroup owns row t of the tile):
+//   layer 1 in two K halves: the thread writes its row's encoding chunks
+//   0..15 (K = 128) into the warpgroup's FP16 tile in shared memory
+//   (K-major core matrices), one thread issues 8 tcgen05.mma (M = 128,
+//   N = 64, K = 16) into the warpgroup's tensor-memory columns and commits
+//   them to the warpgroup's mbarrier; after they complete the same tile takes
+//   chunks 16..29 (K = 112) and 7 more MMAs accumulate;
+//   layers 2..5: every thread reads its row's accumulators (tcgen05.ld),
+//   converts them with ReLU to FP16 (one cvt.rn.relu.f16x2 per pair) into the
+//   next layer's input tile (K = 80: 64 activations, a constant 1 that
+//   carries the bias inside the GEMM, zeros) and the MMAs of that layer run;
+//   the 48 outputs of the row go to global memory, raw or as the packed vMF
+//   mixture the renderer samples.
+// Layer 1's bias rides in encoding column 225, whose input is the constant 1.
+// The weights (68 KB) arrive once per block by bulk copy.  Four warpgroups
+// keep four tiles in flight per SM, so one warpgroup's encoding and
+// epilogues overlap the others' MMAs.  The next tile's features are loaded
+// while the current tile runs.  Every wait is bounded: on timeout the error
+// word gets ERR_TENSOR_TIMEOUT and the block stops, frees its tensor memory
+// and returns.
+constexpr int TC_WG = 4;
+constexpr int TC_THREADS = 128 * TC_WG;
+constexpr int TC_A_BYTES = 128 * 128 * 2;           // one tile of K <= 128
+constexpr int TC_SBO_E0 = 128 * 16;                 // bytes between 8-row groups: encoding chunks 0..15
+constexpr int TC_SBO_E1 = 112 * 16;                 // encoding chunks 16..29
+constexpr int TC_SBO1 = TC_K1 * 16;                 // layer 1's weights (K = 240)
+constexpr int TC_SBOH = TC_KH * 16;                 // K = 80
+constexpr uint32_t TC_COLS = 512;                   // tensor-memory columns per block: 128 per warpgroup
+constexpr uint32_t TC_POLL_LIMIT = 1u << 22;        // polls of a bounded mbarrier wait
+constexpr size_t TC_OFF_A = (size_t)TC_HALVES * 2;
+constexpr size_t TC_OFF_BAR = TC_OFF_A + (size_t)TC_WG * TC_A_BYTES;
+constexpr size_t TC_SMEM = TC_OFF_BAR + 128;
+static_assert(TC_OFF_A % 16 == 0 && TC_OFF_BAR % 8 == 0 && (TC_HALVES * 2) % 16 == 0, "bulk copy / mbarrier alignment");
+static_assert(TC_SMEM <= 227 * 1024, "shared memory of one block");
+static_assert(TC_COLS >= 128u * TC_WG && TC_COLS <= 512u, "tensor memory of one block");
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) { return h2u(__floats2half2_rn(a, b)); }
+// (max(lo, 0), max(hi, 0)) rounded to FP16, lo in the low half
+__device__ __forceinline__ uint32_t pack_relu_h2(float lo, float hi) {
+	uint32_t d;
+	asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+	return d;
+}
+
+// Encoding chunk c (8 halves: pairs 4c .. 4c + 3) of a row.  Pair 12 i + k is
+// (sin, cos)(pi 2^k x_i): chunk c < 27 is feature i = c / 3 at k = 4j .. 4j + 3
+// (j = c % 3), i.e. one evaluation on the special-function unit at k = 4j on
+// the argument reduced to [-1, 1] (2^4j x - 2 rint(2^(4j-1) x) is exact;
+// absolute error about 4e-7 there) and three angle doublings (sin 2a =
+// 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a); error <= 8x).
+// Chunk 27 is the raw features 0..7, chunk 28 (x_8, 1: layer 1's bias input,
+// 0...), chunk 29 zeros.  c must be a compile-time constant after unrolling.
+__device__ __forceinline__ uint4 enc_chunk(const float *x, int c) {
+	if (c < 27) {
+		const int i = c / 3, j = c % 3;
+		const float y = j == 0 ? x[i] : (float)(1 << (4 * j)) * x[i] - 2.0f * rintf((float)(1 << (4 * j - 1)) * x[i]);
+		float sn, cs;
+		__sincosf(3.14159265358979323846f * y, &sn, &cs);
+		uint32_t p[4];
+		p[0] = pack_h2(sn, cs);
 #pragma unroll
-		for (int nt = 0; nt < 6; ++nt) {
-			int col = nt * 8 + 2 * t;
-			if (r0 < n) out[(size_t)r0 * GN_OUT + col] = c5[nt][0], out[(size_t)r0 * GN_OUT + col + 1] = c5[nt][1];
-			if (r1 < n) out[(size_t)r1 * GN_OUT + col] = c5[nt][2], out[(size_t)r1 * GN_OUT + col + 1] = c5[nt][3];
+		for (int k = 1; k < 4; ++k) {
+			const float s2 = 2.f * sn * cs, c2 = (cs - sn) * (cs + sn);
+			sn = s2, cs = c2;
+			p[k] = pack_h2(sn, cs);
 		}
+		return make_uint4(p[0], p[1], p[2], p[3]);
+	}
+	if (c == 27) return make_uint4(pack_h2(x[0], x[1]), pack_h2(x[2], x[3]), pack_h2(x[4], x[5]), pack_h2(x[6], x[7]));
+	if (c == 28) return make_uint4(pack_h2(x[8], 1.0f), 0u, 0u, 0u);
+	return make_uint4(0u, 0u, 0u, 0u);
+}
+
+// one layer's MMAs: D[tcol] (+)= A (128 x 16 ksteps) x W^T, W rows of stride sbo_w
+__device__ __forceinline__ void tc_mmas(uint32_t d_tmem, uint32_t a_addr, uint32_t sbo_a, uint32_t w_addr, uint32_t sbo_w,
+	int ksteps, uint32_t idesc, bool accumulate) {
+	for (int s = 0; s < ksteps; ++s)
+		umma_f16(d_tmem, umma_sdesc(a_addr + 256u * s, 128u, sbo_a), umma_sdesc(w_addr + 256u * s, 128u, sbo_w), idesc,
+			(accumulate || s > 0) ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__restrict__ tc_img,
+	const float *__restrict__ feat, int n, const unsigned *__restrict__ n_dev, float *__restrict__ out,
+	unsigned *__restrict__ err, int mixture_out) {
+	extern __shared__ __align__(16) unsigned char smem[];
+	uint64_t *bar = reinterpret_cast<uint64_t *>(smem + TC_OFF_BAR);  // [0] weights, [1 + wg] MMAs of warpgroup wg
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1 + TC_WG);
+	volatile uint32_t *fail = tmem_slot + 1;  // per warpgroup
+
+	const int tid = threadIdx.x, wg = tid >> 7, lt = tid & 127, warp = tid >> 5;
+	if (n_dev) n = min(n, (int)*n_dev);
+	const int tiles = (n + 127) / 128;
+	const bool out_vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;  // rows are 192 bytes: float4 stores when aligned
+	if (tid == 0) {
+		for (int b = 0; b < 1 + TC_WG; ++b) mbar_init(&bar[b], 1);
+		for (int w = 0; w < TC_WG; ++w) fail[w] = 0;
+		mbar_init_fence();
+	}
+	if (warp == 0) {
+		tmem_alloc(tmem_slot, TC_COLS);
+		tmem_relinquish();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tbase = *tmem_slot;
+	if (tid == 0) {
+		mbar_arrive_expect_tx(&bar[0], (uint32_t)(TC_HALVES * 2));
+		bulk_g2s(smem, tc_img, (uint32_t)(TC_HALVES * 2), &bar[0]);
+	}
+	if (!mbar_wait(&bar[0], 0, TC_POLL_LIMIT)) fail[wg] = 1;
+
+	unsigned char *A = smem + TC_OFF_A + (size_t)wg * TC_A_BYTES;
+	const uint32_t a_addr = smem_addr(A), w_addr = smem_addr(smem);
+	const uint32_t tcol = tbase + (uint32_t)wg * 128u;             // this warpgroup's columns
+	const uint32_t tlane = (uint32_t)((warp & 3) * 32) << 16;      // this warp's lane quarter
+	const uint32_t bar_id = 1 + wg;
+	const uint32_t idesc_h = umma_idesc_f16(128, GN_H), idesc_o = umma_idesc_f16(128, GN_OUT);
+	uint32_t phase = 0;
+	uint64_t *mbar = &bar[1 + wg];
+	unsigned char *e0row = A + (lt >> 3) * TC_SBO_E0 + (lt & 7) * 16;
+	unsigned char *e1row = A + (lt >> 3) * TC_SBO_E1 + (lt & 7) * 16;
+	unsigned char *hrow = A + (lt >> 3) * TC_SBOH + (lt & 7) * 16;
+	// issue the MMAs of `stage` after the tile's writes are visible; false once the warpgroup has failed
+	auto sync_issue = [&](int stage) -> bool {
+		fence_proxy_async_smem();
+		tc_fence_before();
+		named_bar(bar_id, 128);
+		if (fail[wg]) return false;
+		if (lt == 0) {
+			tc_fence_after();
+			if (stage == 0)
+				tc_mmas(tcol, a_addr, TC_SBO_E0, w_addr + TC_W1 * 2, TC_SBO1, 8, idesc_h, false);
+			else if (stage == 1)
+				tc_mmas(tcol, a_addr, TC_SBO_E1, w_addr + TC_W1 * 2 + 256u * 8, TC_SBO1, 7, idesc_h, true);
+			else
+				tc_mmas(tcol + (stage == 5 ? 64u : 0u), a_addr, TC_SBOH,
+					w_addr + (stage == 2 ? TC_W2 : stage == 3 ? TC_W3 : stage == 4 ? TC_W4 : TC_W5) * 2, TC_SBOH, TC_KH / 16,
+					stage == 5 ? idesc_o : idesc_h, false);
+			umma_commit(mbar);
+		}
+		return true;
+	};
+	auto wait_mma = [&]() {
+		if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+		phase ^= 1u;
+		tc_fence_after();
+	};
+	named_bar(bar_id, 128);
+	int tile = blockIdx.x * TC_WG + wg;
+	const int tstep = gridDim.x * TC_WG;
+	float xn[GN_IN];
+#pragma unroll
+	for (int k = 0; k < GN_IN; ++k) xn[k] = (tile * 128 + lt < n) ? feat[(size_t)(tile * 128 + lt) * GN_IN + k] : 0.0f;
+	for (; tile < tiles; tile += tstep) {
+		const int row = tile * 128 + lt;
+		float x[GN_IN];
+#pragma unroll
+		for (int k = 0; k < GN_IN; ++k) x[k] = xn[k];
+		const int nrow = row + tstep * 128;  // prefetch the next tile's features
+#pragma unroll
+		for (int k = 0; k < GN_IN; ++k) xn[k] = nrow < n ? feat[(size_t)nrow * GN_IN + k] : 0.0f;
+		// layer 1, first K half
+#pragma unroll
+		for (int c = 0; c < 16; ++c) *reinterpret_cast<uint4 *>(e0row + c * 128) = enc_chunk(x, c);
+		if (!sync_issue(0)) break;
+		wait_mma();
+		// layer 1, second K half (the tile is free again)
+#pragma unroll
+		for (int c = 16; c < 30; ++c) *reinterpret_cast<uint4 *>(e1row + (c - 16) * 128) = enc_chunk(x, c);
+		if (!sync_issue(1)) break;
+		wait_mma();
+		bool ok = true;
+#pragma unroll 1
+		for (int layer = 2; layer <= 5 && ok; ++layer) {
+			// accumulators of row lt -> ReLU -> FP16 input tile of the next layer, 32 columns at a time
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				uint32_t r[2][16];
+				tmem_ld16(tcol + tlane + 32u * h, r[0]);
+				tmem_ld16(tcol + tlane + 32u * h + 16u, r[1]);
+				tmem_ld_wait();
+#pragma unroll
+				for (int c = 0; c < 4; ++c) {
+					uint32_t w4[4];
+#pragma unroll
+					for (int e = 0; e < 4; ++e) {
+						const int col = 8 * c + 2 * e;
+						w4[e] = pack_relu_h2(__uint_as_float(r[col >> 4][col & 15]), __uint_as_float(r[col >> 4][(col & 15) + 1]));
+					}
+					*reinterpret_cast<uint4 *>(hrow + (4 * h + c) * 128) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+				}
+			}
+			if (layer == 2) {
+				*reinterpret_cast<uint4 *>(hrow + 8 * 128) = make_uint4(pack_h2(1.f, 0.f), 0u, 0u, 0u);
+				*reinterpret_cast<uint4 *>(hrow + 9 * 128) = make_uint4(0u, 0u, 0u, 0u);
+			}
+			ok = sync_issue(layer);
+			if (ok) wait_mma();
+		}
+		if (!ok) break;
+		uint32_t r[3][16];
+#pragma unroll
+		for (int g = 0; g < 3; ++g) tmem_ld16(tcol + 64u + tlane + 16u * g, r[g]);
+		tmem_ld_wait();
+		if (row < n && mixture_out) {
+			// the vMF mixture of the row, packed for the renderer (out is 16-byte aligned there)
+			float o[5 * GN_LOBES];
+#pragma unroll
+			for (int col = 0; col < 5 * GN_LOBES; ++col) o[col] = __uint_as_float(r[col >> 4][col & 15]);
+			Mixture M;
+			to_mixture(o, M);
+			float pk[GN_OUT];
+			store_mixture(M, pk);
+			float4 *dst = reinterpret_cast<float4 *>(out + (size_t)row * GN_OUT);
+#pragma unroll
+			for (int q = 0; q < GN_OUT / 4; ++q) dst[q] = make_float4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+		} else if (row < n) {
+			float *orow = out + (size_t)row * GN_OUT;
+			if (out_vec) {
+				float4 *o = reinterpret_cast<float4 *>(orow);
+#pragma unroll
+				for (int q = 0; q < GN_OUT / 4; ++q) {
+					const int col = 4 * q;
+					o[q] = make_float4(__uint_as_float(r[col >> 4][col & 15]), __uint_as_float(r[col >> 4][(col & 15) + 1]),
+						__uint_as_float(r[col >> 4][(col & 15) + 2]), __uint_as_float(r[col >> 4][(col & 15) + 3]));
+				}
+			} else {
+#pragma unroll
+				for (int col = 0; col < GN_OUT; ++col) orow[col] = __uint_as_float(r[col >> 4][col & 15]);
+			}
+		}
+		tc_fence_before();
+	}
+	named_bar(bar_id, 128);
+	if (lt == 0 && fail[wg]) {
+		atomicOr(err, (unsigned)ERR_TENSOR_TIMEOUT);
+		// let work still in flight land before the memory is released
+		mbar_wait(&bar[0], 0, TC_POLL_LIMIT);
+		mbar_wait(mbar, phase ^ 1u, TC_POLL_LIMIT);
+	}
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 0) {
+		tc_fence_after();
+		tmem_dealloc(tbase, TC_COLS);
 	}
 }
 
@@ -386,10 +638,6 @@ __global__ void k_weight_scale(const float *__restrict__ samples, int n, float *
 	if (threadIdx.x == 0) *out = red[0] > 0.f ? (float)n / red[0] : 0.f;
 }
 
-__global__ void k_scale_copy(const float *__restrict__ g, float s, float *__restrict__ out, int n) {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = g[i] * s;
-}
-
 are_status bad(const std::string &m) {
 	set_error(m);
 	return ARE_ERR_INVALID_ARGUMENT;
@@ -397,7 +645,7 @@ are_status bad(const std::string &m) {
 
 }  // namespace
 
-size_t guide_infer_smem() { return IMG_FWD * sizeof(__half) + IMG_BIAS * sizeof(float); }
+size_t guide_infer_smem() { return TC_SMEM; }
 size_t guide_train_smem() {
 	return IMG_ALL * sizeof(__half) + IMG_BIAS * sizeof(float) + (GT / 32) * 16 * GN_OUT * sizeof(float) +
 		(GT / 32) * 16 * S_OUT * sizeof(__half);
@@ -426,6 +674,8 @@ are_status GuideNet::init(uint64_t seed) {
 	if (are_status st = alloc((void **)&grad, (GN_PARAMS + 64) * sizeof(float))) return st;
 	if (are_status st = alloc((void **)&img, IMG_ALL * sizeof(__half))) return st;
 	if (are_status st = alloc((void **)&bias, IMG_BIAS * sizeof(float))) return st;
+	if (are_status st = alloc((void **)&tc_img, TC_HALVES * sizeof(__half))) return st;
+	if (are_status st = alloc((void **)&err_word, 16)) return st;
 	if (cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_infer_smem()) != cudaSuccess ||
 		cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_train_smem()) != cudaSuccess)
 		return cuda_status(cudaGetLastError(), "cudaFuncSetAttribute(guide)");
@@ -462,6 +712,7 @@ are_status GuideNet::set_params(const float *host) {
 
 are_status GuideNet::pack() {
 	k_guide_pack<<<128, 256, 0, stream>>>(params, img, bias);
+	k_guide_pack_tc<<<68, 256, 0, stream>>>(params, tc_img);
 	return cuda_status(cudaGetLastError(), "k_guide_pack");
 }
 
@@ -484,13 +735,15 @@ are_status GuideNet::ensure_train(int n) {
 	return ARE_OK;
 }
 
-are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev) {
+are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev,
+	unsigned *d_err, bool mixture_out) {
+	if (mixture_out && (reinterpret_cast<uintptr_t>(d_out) & 15)) return bad("mixture output must be 16-byte aligned");
 	if (n <= 0) return ARE_OK;
-	int per_sm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_guide_infer, GT, guide_infer_smem());
-	int grid = std::max(1, per_sm) * n_sms;
-	grid = std::min(grid, ((n + 15) / 16 + 7) / 8);
-	k_guide_infer<<<grid, GT, guide_infer_smem(), s>>>(img, bias, d_feat, n, n_dev, d_out);
+	// one block per SM (its shared memory allows no second); two 128-row tiles per block in flight
+	const int tiles = (n + 127) / 128;
+	const int grid = std::max(1, std::min(n_sms, (tiles + TC_WG - 1) / TC_WG));
+	k_guide_infer<<<grid, TC_THREADS, guide_infer_smem(), s>>>(tc_img, d_feat, n, n_dev, d_out, d_err ? d_err : err_word,
+		mixture_out ? 1 : 0);
 	return cuda_status(cudaGetLastError(), "k_guide_infer");
 }
 
@@ -532,6 +785,7 @@ are_status GuideNet::train_step(const float *d_samples, int n, float wmean, floa
 	k_guide_adam<<<64, 256, 0, s>>>(params, adam_m, adam_v, grad, 1.0f / (loss_scale * (float)n), lr, 0.9f, 0.99f, 1e-8f,
 		c1, c2, (const unsigned *)(grad + GN_PARAMS + 1));
 	k_guide_pack<<<128, 256, 0, s>>>(params, img, bias);
+	k_guide_pack_tc<<<68, 256, 0, s>>>(params, tc_img);
 	return cuda_status(cudaGetLastError(), "guide Adam");
 }
 
@@ -625,12 +879,45 @@ ARE_API are_status are_guide_forward(are_guide *gh, const float *features, int64
 		if (!g || (n > 0 && (!features || !out)) || n < 0 || n > (1 << 26)) return are_core::bad("bad guide forward arguments");
 		if (n == 0) return ARE_OK;
 		DevTmp t;
-		size_t fb = (size_t)n * are_core::GN_IN * 4, ob = (size_t)n * are_core::GN_OUT * 4;
+		// outputs start on a 256-byte boundary after the features (the kernel stores rows as float4)
+		size_t fb = ((size_t)n * are_core::GN_IN * 4 + 255) & ~(size_t)255, ob = (size_t)n * are_core::GN_OUT * 4;
 		if (are_status st = are_core::cuda_status(cudaMalloc(&t.p, fb + ob), "cudaMalloc")) return st;
-		cudaMemcpyAsync(t.p, features, fb, cudaMemcpyHostToDevice, g->stream);
+		cudaMemcpyAsync(t.p, features, (size_t)n * are_core::GN_IN * 4, cudaMemcpyHostToDevice, g->stream);
+		cudaMemsetAsync(g->err_word, 0, 4, g->stream);
 		if (are_status st = g->infer((const float *)t.p, (int)n, (float *)((char *)t.p + fb), g->stream)) return st;
 		cudaMemcpyAsync(out, (char *)t.p + fb, ob, cudaMemcpyDeviceToHost, g->stream);
-		return are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide forward");
+		unsigned herr = 0;
+		cudaMemcpyAsync(&herr, g->err_word, 4, cudaMemcpyDeviceToHost, g->stream);
+		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide forward")) return st;
+		if (herr) {
+			are_core::set_error("guide forward: device error word " + std::to_string(herr));
+			return ARE_ERR_KERNEL_TIMEOUT;
+		}
+		return ARE_OK;
+	});
+}
+
+ARE_API are_status are_guide_mixture(are_guide *gh, const float *features, int64_t n, float *out) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g || (n > 0 && (!features || !out)) || n < 0 || n > (1 << 26)) return are_core::bad("bad guide mixture arguments");
+		if (n == 0) return ARE_OK;
+		DevTmp t;
+		size_t fb = ((size_t)n * are_core::GN_IN * 4 + 255) & ~(size_t)255, ob = (size_t)n * are_core::GN_OUT * 4;
+		if (are_status st = are_core::cuda_status(cudaMalloc(&t.p, fb + ob), "cudaMalloc")) return st;
+		cudaMemcpyAsync(t.p, features, (size_t)n * are_core::GN_IN * 4, cudaMemcpyHostToDevice, g->stream);
+		cudaMemsetAsync(g->err_word, 0, 4, g->stream);
+		if (are_status st = g->infer((const float *)t.p, (int)n, (float *)((char *)t.p + fb), g->stream, nullptr, nullptr, true))
+			return st;
+		cudaMemcpyAsync(out, (char *)t.p + fb, ob, cudaMemcpyDeviceToHost, g->stream);
+		unsigned herr = 0;
+		cudaMemcpyAsync(&herr, g->err_word, 4, cudaMemcpyDeviceToHost, g->stream);
+		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide mixture")) return st;
+		if (herr) {
+			are_core::set_error("guide mixture: device error word " + std::to_string(herr));
+			return ARE_ERR_KERNEL_TIMEOUT;
+		}
+		return ARE_OK;
 	});
 }
 

@@ -42,6 +42,28 @@ constexpr int IMG_W5T = IMG_W4T + GN_H * S_H;      // [64 in][S_OUT]
 constexpr int IMG_ALL = IMG_W5T + GN_H * S_OUT;    // halves of forward + backward image
 constexpr int IMG_BIAS = 4 * GN_H + GN_OUT;        // FP32 biases after the halves
 
+// Weight image of the tcgen05 inference kernel (halves): each layer's
+// [out][in] matrix in the canonical no-swizzle K-major layout of the tensor
+// core (core matrices of 8 rows x 8 halves, 64 halves each; the core matrices
+// of one 8-row group adjacent in K).  The biases ride in the GEMMs: layer 1
+// keeps K = 240 (encoding columns 240..255 are always zero) and takes its
+// bias in column 225, whose input is the constant 1 (the encoding is zero
+// there); the other layers get K = 80, column 64 the bias against a constant
+// 1 input, columns 65..79 zero.
+constexpr int TC_K1 = 240;
+constexpr int TC_KH = 80;
+constexpr int TC_ONE1 = 225;                    // constant-1 input column of layer 1
+constexpr int TC_W1 = 0;                        // [64][240]
+constexpr int TC_W2 = TC_W1 + GN_H * TC_K1;     // [64][80]
+constexpr int TC_W3 = TC_W2 + GN_H * TC_KH;
+constexpr int TC_W4 = TC_W3 + GN_H * TC_KH;
+constexpr int TC_W5 = TC_W4 + GN_H * TC_KH;     // [48][80]
+constexpr int TC_HALVES = TC_W5 + GN_OUT * TC_KH;
+// index of element (row, k) of a K-column matrix in that layout
+__host__ __device__ constexpr int tc_index(int row, int k, int K) {
+	return (row >> 3) * (K * 8) + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+}
+
 // features of a shading point: position scaled to the scene box, normal, outgoing direction
 struct GuideBox {
 	float lo[3], inv_ext[3];
@@ -55,18 +77,37 @@ __device__ __forceinline__ void guide_features(const GuideBox &B, f3 p, f3 n, f3
 	x[6] = wo.x, x[7] = wo.y, x[8] = wo.z;
 }
 
-// encoding pair index 0..127 -> two consecutive encoding values
-__device__ __forceinline__ __half2 enc_pair(const float *x, int pi) {
-	if (pi < 108) {
-		int i = pi / 12, k = pi - 12 * (pi / 12);
-		float s, c;
-		sincospif(ldexpf(x[i], k), &s, &c);
+// The input encoding is 128 pairs of FP16 values: pair 12 i + k (i < 9,
+// k < 12) is (sin, cos)(pi 2^k x_i), pairs 108..112 the raw features two by
+// two (the last one padded with 0), the rest zero.
+//
+// Lane t of a quad holds pair indices b + t with b a
+// multiple of 4 (a constant once the caller's loop is unrolled).  For b < 108
+// that is feature i = b / 12 at frequency k = b % 12 + t, and b % 12 runs
+// through 0, 4, 8 for each feature in turn.  Frequencies t and t + 8 take a
+// sincospif each; t + 4 comes from t by four angle doublings (sin 2a =
+// 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a)), which grow the FP32
+// rounding error 16-fold, to about 2e-5: below the FP16 rounding of the result.
+__device__ __forceinline__ __half2 enc_quad(const float *x, int b, int t, float &s, float &c) {
+	if (b < 108) {
+		const int i = b / 12;
+		if (b % 12 != 4) {
+			sincospif(ldexpf(x[i], t + b % 12), &s, &c);
+		} else {
+#pragma unroll
+			for (int d = 0; d < 4; ++d) {  // 2^4: angle doublings from k to k + 4
+				float s2 = 2.f * s * c, c2 = (c - s) * (c + s);
+				s = s2, c = c2;
+			}
+		}
 		return __floats2half2_rn(s, c);
 	}
-	if (pi < 113) {
-		int m = 2 * (pi - 108);
-		return __floats2half2_rn(x[m], m + 1 < GN_IN ? x[m + 1] : 0.0f);
+	if (b == 108) {  // raw features (x[2t], x[2t+1])
+		float u = t == 0 ? x[0] : t == 1 ? x[2] : t == 2 ? x[4] : x[6];
+		float v = t == 0 ? x[1] : t == 1 ? x[3] : t == 2 ? x[5] : x[7];
+		return __floats2half2_rn(u, v);
 	}
+	if (b == 112) return __floats2half2_rn(t == 0 ? x[8] : 0.0f, 0.0f);
 	return __floats2half2_rn(0.0f, 0.0f);
 }
 
@@ -146,6 +187,35 @@ __device__ __forceinline__ void to_mixture(const float *o, Mixture &m) {
 	for (int l = 0; l < GN_LOBES; ++l) m.pi[l] *= iz;
 }
 
+// The packed form the inference kernel writes for rendering (48 floats per
+// row): lobe l's (mu.x, mu.y, mu.z, kappa) at 4 l, then (pi_l, norm_l) at
+// 32 + 2 l.
+// The mean directions are stored at unit length (to_mixture divides by
+// |m| + 1e-6): mixture_sample draws around a unit axis, so the density the
+// renderer reports is then exactly the density it samples.
+__device__ __forceinline__ void store_mixture(const Mixture &m, float *o) {
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) {
+		const f3 a = m.mu[l];
+		const float len2 = a.x * a.x + a.y * a.y + a.z * a.z;
+		const f3 u = len2 > 0.f ? scl(a, rsqrtf(len2)) : f3{ 0.f, 0.f, 1.f };
+		const float r = rsqrtf(u.x * u.x + u.y * u.y + u.z * u.z);  // a second pass: unit within an ulp or two
+		o[4 * l] = u.x * r, o[4 * l + 1] = u.y * r, o[4 * l + 2] = u.z * r, o[4 * l + 3] = m.kappa[l];
+		o[32 + 2 * l] = m.pi[l], o[33 + 2 * l] = m.norm[l];
+	}
+}
+__device__ __forceinline__ void load_mixture(const float *__restrict__ o, Mixture &m) {
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) {
+		const float4 a = reinterpret_cast<const float4 *>(o)[l];
+		const float2 b = reinterpret_cast<const float2 *>(o + 32)[l];
+		m.mu[l] = f3{ a.x, a.y, a.z };
+		m.kappa[l] = a.w;
+		m.pi[l] = b.x;
+		m.norm[l] = b.y;
+	}
+}
+
 __device__ __forceinline__ float mixture_pdf(const Mixture &m, f3 w) {
 	float q = 0.f;
 #pragma unroll
@@ -159,16 +229,21 @@ __device__ __forceinline__ float mixture_pdf(const Mixture &m, f3 w) {
 // Draw a direction: lobe by u0, then the vMF sample of W. Jakob's stable form
 // cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) / kappa, azimuth 2 pi u2.
 __device__ __forceinline__ f3 mixture_sample(const Mixture &m, float u0, float u1, float u2) {
-	int l = 0;
-	float acc = m.pi[0];
-	while (l < GN_LOBES - 1 && u0 >= acc) acc += m.pi[++l];
-	float k = m.kappa[l];
+	// the first lobe whose cumulative weight exceeds u0 (the last one if
+	// rounding leaves u0 above the total), selected without dynamic indexing
+	f3 z = m.mu[GN_LOBES - 1];
+	float k = m.kappa[GN_LOBES - 1], acc = 0.f;
+	bool found = false;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES - 1; ++l) {
+		acc += m.pi[l];
+		if (!found && u0 < acc) z = m.mu[l], k = m.kappa[l], found = true;
+	}
 	float w = 1.f + logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k;
 	w = fminf(fmaxf(w, -1.f), 1.f);
 	float r = sqrtf(fmaxf(0.f, 1.f - w * w));
 	float s, c;
 	sincospif(2.f * u2, &s, &c);
-	f3 z = m.mu[l];
 	f3 up = fabsf(z.z) < 0.999f ? f3{ 0.f, 0.f, 1.f } : f3{ 1.f, 0.f, 0.f };
 	f3 x = norm(cross(z, up));
 	f3 y = cross(z, x);

@@ -28,8 +28,10 @@ struct GuideNet {
 	bool own_stream = false;
 	float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr;
 	float *grad = nullptr;  // GN_PARAMS gradients, then loss sum, then an overflow flag
-	__half *img = nullptr;
+	__half *img = nullptr;     // FP16 weights for the training kernels (row-major, padded strides)
+	__half *tc_img = nullptr;  // FP16 weights for the tensor-core inference kernel (core-matrix layout)
 	float *bias = nullptr;
+	unsigned *err_word = nullptr;  // device error bits of inference outside a render
 	void *train_mem = nullptr;
 	int train_cap = 0;
 	GuideTrainBufs bufs{};
@@ -45,7 +47,10 @@ struct GuideNet {
 	are_status pack();
 	are_status ensure_train(int n);
 	// n_dev: optional device row count (rows = min(n, *n_dev)), read when the kernel runs
-	are_status infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev = nullptr);
+	// d_err: device error word to OR failures into (default: err_word)
+	// mixture_out: write the packed vMF mixture (store_mixture) instead of the raw outputs
+	are_status infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev = nullptr,
+		unsigned *d_err = nullptr, bool mixture_out = false);
 	// wmean < 0: normalise the weights by their batch mean computed on the device
 	are_status gradient(const float *d_samples, int n, float wmean, cudaStream_t s);
 	are_status train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s);

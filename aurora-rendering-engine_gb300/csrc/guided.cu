@@ -28,6 +28,8 @@
 namespace are_core {
 
 constexpr int GV = 4;  // guided vertices recorded per path (the first diffuse bounces)
+// iterations per graph launch; training steps are taken between launches
+constexpr int GUIDED_ITERS = 8;
 
 struct GuidedState {
 	int32_t *gidx;        // per queue position: row in the compact list or -1
@@ -96,11 +98,19 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 		bool cont = false, term = false;
 		f3 p, nd, beta, L;
 		float4 ra, rb, rc;
+		// qd.w packs the path's roulette scale (a positive float, low 4 mantissa
+		// bits dropped; 0 at the camera means 1) with the recorded-vertex mask:
+		// bit v set = guided vertex v of this path is recorded in vrec
+		unsigned vmask = 0;
+		float rrs = 1.0f;
 		if (valid) {
 			ra = W.qa[par][i];
 			rb = W.qb[par][i];
 			rc = W.qc[par][i];
 			float4 rd = W.qd[par][i];
+			const unsigned packed = __float_as_uint(rd.w);
+			vmask = packed & 0xfu;
+			if (packed & ~0xfu) rrs = __uint_as_float(packed & ~0xfu);
 			float4 h = W.hit[i];
 			beta = ld3(rc);
 			L = ld3(rd);
@@ -124,11 +134,8 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 				int gi = G.gidx[i];
 				if (gi >= 0) {
 					// guided diffuse vertex: one-sample MIS of the vMF mixture and cosine sampling
-					float ov[40];
-#pragma unroll
-					for (int k = 0; k < 40; ++k) ov[k] = G.gout[(size_t)gi * GN_OUT + k];
 					Mixture M;
-					to_mixture(ov, M);
+					load_mixture(G.gout + (size_t)gi * GN_OUT, M);
 					f3 nrm = dot(d, sf.ng) < 0.f ? sf.ng : scl(sf.ng, -1.f);
 					uint32_t cb = ctr_bounce(depth);
 					f3 w;
@@ -148,11 +155,13 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 						const DevMaterial &m = S.mats[sf.mat];
 						f3 alb = tex_eval(S, m.texture, sf.u, sf.v, sf.p);
 						f3 L_before = L;
-						beta = mulv(beta, scl(alb, cosw * inv_pi / pdf));
+						const float ratio = cosw * inv_pi / pdf;  // cosine-sampling pdf over the MIS pdf
+						beta = mulv(beta, scl(alb, ratio));
+						rrs = fminf(fmaxf(rrs / ratio, 1e-30f), 1e30f);
 						nd = w;
 						cont = true;
 						if (W.rr_depth >= 0 && depth >= W.rr_depth) {
-							float q = fmaxf(fmaxf(beta.x, beta.y), beta.z);
+							float q = fmaxf(fmaxf(beta.x, beta.y), beta.z) * rrs;
 							if (q < 1.0f) {
 								if (uniform(key, cb + 3) >= q)
 									cont = false;
@@ -169,13 +178,14 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 							v[0] = make_float4(x[0], x[1], x[2], x[3]);
 							v[1] = make_float4(x[4], x[5], x[6], x[7]);
 							v[2] = make_float4(x[8], w.x, w.y, w.z);
-							v[3] = make_float4(pdf, cosw, 1.f, 0.f);
+							v[3] = make_float4(pdf, cosw, 0.f, 0.f);
 							v[4] = make_float4(beta.x, beta.y, beta.z, 0.f);
 							v[5] = make_float4(L_before.x, L_before.y, L_before.z, 0.f);
+							vmask |= 1u << depth;
 						}
 					}
 				} else {
-					cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd);
+					cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd, rrs);
 				}
 				if (cont && depth + 1 >= W.max_depth) cont = false;
 				p = sf.p;
@@ -188,7 +198,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 				W.qa[out][pos] = make_float4(p.x, p.y, p.z, ra.w);
 				W.qb[out][pos] = make_float4(nd.x, nd.y, nd.z, __int_as_float(__float_as_int(rb.w) + 1));
 				W.qc[out][pos] = make_float4(beta.x, beta.y, beta.z, rc.w);
-				W.qd[out][pos] = make_float4(L.x, L.y, L.z, 0.f);
+				W.qd[out][pos] = make_float4(L.x, L.y, L.z, __uint_as_float((__float_as_uint(rrs) & ~0xfu) | vmask));
 			} else {
 				err |= ERR_QUEUE_OVERFLOW;
 			}
@@ -197,7 +207,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 		if (term) {
 			if (tp < (unsigned)W.P) {
 				W.ta[tp] = make_float4(L.x, L.y, L.z, ra.w);
-				W.tb[tp] = make_float4(rc.w, __int_as_float(__float_as_int(rb.w) >> 8), 0.f, 0.f);
+				W.tb[tp] = make_float4(rc.w, __int_as_float(__float_as_int(rb.w) >> 8), __uint_as_float(vmask), 0.f);
 			} else {
 				err |= ERR_QUEUE_OVERFLOW;
 			}
@@ -215,14 +225,12 @@ __global__ void __launch_bounds__(BLOCK) k_emit_training(Wave W, GuidedState G) 
 		for (int v = 0; v < GV; ++v) {
 			bool emit = false;
 			float rec[13];
-			if (i < n) {
+			if (i < n && ((__float_as_uint(W.tb[i].z) >> v) & 1u)) {
 				float4 a = W.ta[i];
 				int slot = __float_as_int(a.w);
-				float4 *r = G.vrec + ((size_t)slot * GV + v) * 6;
-				float4 r3 = r[3];
-				if (r3.z != 0.f) {
-					float4 r0 = r[0], r1 = r[1], r2 = r[2], r4 = r[4], r5 = r[5];
-					r[3] = make_float4(0.f, 0.f, 0.f, 0.f);  // consumed
+				const float4 *r = G.vrec + ((size_t)slot * GV + v) * 6;
+				{
+					float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4], r5 = r[5];
 					// incident radiance estimate along the sampled direction
 					float li[3] = { r4.x > 0.f ? (a.x - r5.x) / r4.x : 0.f, r4.y > 0.f ? (a.y - r5.y) / r4.y : 0.f,
 						r4.z > 0.f ? (a.z - r5.z) / r4.z : 0.f };
@@ -241,8 +249,11 @@ __global__ void __launch_bounds__(BLOCK) k_emit_training(Wave W, GuidedState G) 
 			unsigned m = __ballot_sync(0xffffffffu, emit);
 			if (lane_id_g() == 0 && m) atomicAdd(&W.stat[2], (unsigned long long)__popc(m));
 			if (emit && pos < G.tcap) {
-				float *o = G.tbuf + (size_t)pos * 16;
-				for (int k = 0; k < 13; ++k) o[k] = rec[k];
+				float4 *o = reinterpret_cast<float4 *>(G.tbuf + (size_t)pos * 16);
+				o[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
+				o[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
+				o[2] = make_float4(rec[8], rec[9], rec[10], rec[11]);
+				o[3] = make_float4(rec[12], 0.f, 0.f, 0.f);
 			}
 		}
 	}
@@ -274,6 +285,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		return bad("width, height, spp must be > 0 and max_depth in [1, 255]");
 	if (!(gp->mix >= 0.f && gp->mix <= 1.f)) return bad("mix must be in [0, 1]");
 	if (gp->guide_depth < 0 || gp->guide_depth > GV) return bad("guide_depth must be in [0, 4]");
+	if (gp->train < 0 || gp->train > 16) return bad("train must be in [0, 16]");
 	if (gp->train && (gp->batch < 256 || gp->batch > (1 << 20) || !(gp->lr > 0.f))) return bad("bad training batch or lr");
 	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");
 	if (net->device != sc->device) return bad("guide and scene live on different devices");
@@ -357,7 +369,6 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	cudaEventRecord(ev0, s);
 	are_status st = cuda_status(cudaMemcpyAsync(W.cnt, init, sizeof init, cudaMemcpyHostToDevice, s), "counters");
 	if (!st) st = cuda_status(cudaMemsetAsync(W.stat, 0, 64, s), "stats");
-	if (!st) st = cuda_status(cudaMemsetAsync(G.vrec, 0, (size_t)P * GV * 6 * sizeof(float4), s), "vrec");
 	if (!st) {
 		k_init<<<grid_of((const void *)k_init, sc->n_sms), BLOCK, 0, s>>>(W, (int)init[0]);
 		++launches[ARE_KERNEL_OTHER];
@@ -372,12 +383,12 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	// the network runs on the compact list, its length read on the device
 	if (!st) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
 	if (!st) {
-		for (int it = 0; it < GRAPH_ITERS; ++it) {
+		for (int it = 0; it < GUIDED_ITERS; ++it) {
 			int par = it & 1;
 			k_intersect<<<g_int, BLOCK, 0, s>>>(S, W, par);
 			cudaMemsetAsync(W.cnt + 6, 0, 4, s);
 			k_guide_select<<<g_sel, BLOCK, 0, s>>>(S, W, G, par);
-			net->infer(G.gfeat, P, G.gout, s, W.cnt + 6);
+			net->infer(G.gfeat, P, G.gout, s, W.cnt + 6, W.cnt + 4, true);
 			k_shade_guided<<<g_sh, BLOCK, 0, s>>>(S, W, G, par);
 			k_emit_training<<<g_emit, BLOCK, 0, s>>>(W, G);
 			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
@@ -388,31 +399,37 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	const int64_t max_launches = (int64_t)(W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk + 16;
 	unsigned *hc = sc->host_counters;
 	bool pending_loss = false;
+	unsigned pending_n = 1;
+	// a step needs a quarter batch: fewer samples make a noisy gradient
+	const unsigned tmin = std::max(256u, tcap / 4);
 	for (int64_t g = 0; !st; ++g) {
 		st = cuda_status(cudaGraphLaunch(exec, s), "graph launch");
 		if (st) break;
 		cudaMemcpyAsync(hc, W.cnt, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
 		st = cuda_status(cudaStreamSynchronize(s), "guided iteration");
 		if (st) break;
-		iterations += GRAPH_ITERS;
-		launches[ARE_KERNEL_INTERSECT] += GRAPH_ITERS;
-		launches[ARE_KERNEL_SHADE] += 3 * GRAPH_ITERS;
-		launches[ARE_KERNEL_GENERATE] += 2 * GRAPH_ITERS;
-		unsigned have = hc[7];
+		iterations += GUIDED_ITERS;
+		launches[ARE_KERNEL_INTERSECT] += GUIDED_ITERS;
+		launches[ARE_KERNEL_SHADE] += 3 * GUIDED_ITERS;
+		launches[ARE_KERNEL_GENERATE] += 2 * GUIDED_ITERS;
+		const unsigned have = std::min(hc[7], tcap);
 		if (pending_loss) {
 			// the loss of the step enqueued after the previous launch is complete now
-			net->loss_log.push_back(hc[16 + 0] == 0 ? 0.f : *reinterpret_cast<float *>(&hc[16]) / (float)tcap);
+			net->loss_log.push_back(*reinterpret_cast<float *>(&hc[16]) / (float)pending_n);
 			pending_loss = false;
 		}
-		if (gp->train && have >= tcap) {
-			// one Adam step on the collected batch, then collect again
+		if (gp->train && have >= tmin) {
+			// `train` Adam steps on what was collected (up to one batch), then collect again
 			net->weight_clip = gp->weight_clip > 0.f ? gp->weight_clip : 1e30f;
-			st = net->train_step(G.tbuf, (int)tcap, -1.0f, gp->lr, s);
+			for (int k = 0; k < gp->train && !st; ++k) {
+				st = net->train_step(G.tbuf, (int)have, -1.0f, gp->lr, s);
+				++train_steps;
+				launches[ARE_KERNEL_OTHER] += 7;
+			}
 			cudaMemcpyAsync(hc + 16, net->grad + GN_PARAMS, 4, cudaMemcpyDeviceToHost, s);
 			pending_loss = true;
+			pending_n = have;
 			cudaMemsetAsync(G.tcount, 0, 4, s);
-			++train_steps;
-			launches[ARE_KERNEL_OTHER] += 6;
 		}
 		if (hc[0] == 0) break;
 		if (g > max_launches) {
@@ -438,7 +455,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		}
 		st = cuda_status(cudaStreamSynchronize(s), "guided render");
 	}
-	if (!st && pending_loss) net->loss_log.push_back(*reinterpret_cast<float *>(&hc[16]) / (float)tcap);
+	if (!st && pending_loss) net->loss_log.push_back(*reinterpret_cast<float *>(&hc[16]) / (float)pending_n);
 	float ms = 0.f;
 	cudaEventElapsedTime(&ms, ev0, ev1);
 	if (exec) cudaGraphExecDestroy(exec);

@@ -156,17 +156,15 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	}
 	const int g_int = blocks_for((const void *)k_intersect, sc->n_sms);
 	const int g_sh = blocks_for((const void *)k_shade, sc->n_sms);
-	const int g_gen = blocks_for((const void *)k_generate, sc->n_sms);
 	const int64_t max_rounds = (W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk / GRAPH_ITERS + 16;
 	for (int64_t round = 0; !st; ++round) {
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
 			int par = it & 1;
 			k_intersect<<<g_int, BLOCK, 0, s>>>(sc->dev, W, par);
 			k_shade<<<g_sh, BLOCK, 0, s>>>(sc->dev, W, par);
-			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
 		}
 		iterations += GRAPH_ITERS;
-		for (int k = 0; k < 3; ++k) launches[k] += GRAPH_ITERS;
+		for (int k = 0; k < 2; ++k) launches[k] += GRAPH_ITERS;
 		st = cuda_status(cudaGetLastError(), "wavefront launch");
 		if (st) break;
 		st = cuda_status(cudaMemcpyAsync(hc, W.cnt, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "counters");

@@ -144,16 +144,56 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
+// Kahan accumulation of a finished path's radiance L into its slot, in sample
+// order; when the slot's work item is complete its sums are published and the
+// slot takes the next item from *next_item.  Returns whether the slot has a
+// next sample (item, j).
+__device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64_t &item, int &j, uint32_t &err,
+	unsigned *next_item) {
+	if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
+		err |= ERR_NONFINITE;
+		L = f3{ 0.f, 0.f, 0.f };
+	}
+	float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
+	float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
+	float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
+	cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
+	sm = make_float4(ts[0], ts[1], ts[2], 0.f);
+	q = make_float4(q.x + L.x * L.x, q.y + L.y * L.y, q.z + L.z * L.z, 0.f);
+	++j;
+	int chunk_len = min(W.chunk, W.spp - (int)((uint32_t)item / (uint32_t)W.npix) * W.chunk);
+	if (j >= chunk_len) {
+		// item complete: publish its sums, take the next item
+		W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
+		W.item_q[item] = q;
+		sm = cm = q = make_float4(0.f, 0.f, 0.f, 0.f);
+		item = (int64_t)atomicAdd(next_item, 1u);
+		j = 0;
+	}
+	W.acc_s[slot] = sm;
+	W.acc_c[slot] = cm;
+	W.acc_q[slot] = q;
+	return item < W.n_items;
+}
+
+// One bounce of every queued path, fused with the accumulate and generate
+// steps: a path that continues is appended to the next queue; a path that
+// ends adds its radiance to its slot (finish_path) and, if the slot has a
+// next sample, that sample's camera ray takes its place in the next queue.
+// One warp-aggregated append serves both.
 __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 	const unsigned n = W.cnt[par];
 	const int out = par ^ 1;
 	uint32_t err = 0;
+	unsigned long long done = 0;
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		unsigned i = base + threadIdx.x;
 		bool valid = i < n;
-		bool cont = false, term = false;
+		bool cont = false, spawn = false;
 		f3 p, nd, beta, L;
 		float4 ra, rb, rc;
+		int64_t item = 0;
+		int j = 0;
 		if (valid) {
 			ra = W.qa[par][i];
 			rb = W.qb[par][i];
@@ -163,47 +203,50 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 			beta = ld3(rc);
 			L = ld3(rd);
 			int meta = __float_as_int(rb.w);
-			int depth = meta & 0xff, j = meta >> 8;
+			int depth = meta & 0xff;
+			j = meta >> 8;
+			item = (int64_t)(unsigned)__float_as_int(rc.w);
 			f3 o = ld3(ra), d = ld3(rb);
 			int leaf = __float_as_int(h.y);
 			if (leaf < 0) {
 				L = add(L, mulv(beta, background(S, d)));
 			} else {
 				int pixel, sample;
-				item_coords(W, (int64_t)(unsigned)__float_as_int(rc.w), j, pixel, sample);
+				item_coords(W, item, j, pixel, sample);
 				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
 				Surface sf = surface_at(S, leaf, o, d, h.x, h.z, h.w);
 				cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd);
 				if (cont && depth + 1 >= W.max_depth) cont = false;
 				p = sf.p;
 			}
-			term = !cont;
+			if (!cont) {
+				++done;
+				spawn = finish_path(W, __float_as_int(ra.w), L, item, j, err, &W.cnt[3]);
+			}
 		}
-		unsigned pos = warp_append(&W.cnt[out], cont);
-		if (cont) {
-			if (pos < (unsigned)W.P) {
+		unsigned pos = warp_append(&W.cnt[out], cont || spawn);
+		if (cont || spawn) {
+			if (pos >= (unsigned)W.P) {
+				err |= ERR_QUEUE_OVERFLOW;
+			} else if (cont) {
 				int meta = __float_as_int(rb.w) + 1;  // depth + 1, same sample
 				W.qa[out][pos] = make_float4(p.x, p.y, p.z, ra.w);
 				W.qb[out][pos] = make_float4(nd.x, nd.y, nd.z, __int_as_float(meta));
 				W.qc[out][pos] = make_float4(beta.x, beta.y, beta.z, rc.w);
 				W.qd[out][pos] = make_float4(L.x, L.y, L.z, 0.f);
 			} else {
-				err |= ERR_QUEUE_OVERFLOW;
-			}
-		}
-		unsigned tp = warp_append(&W.cnt[2], term);
-		if (term) {
-			if (tp < (unsigned)W.P) {
-				W.ta[tp] = make_float4(L.x, L.y, L.z, ra.w);
-				W.tb[tp] = make_float4(rc.w, __int_as_float(__float_as_int(rb.w) >> 8), 0.f, 0.f);
-			} else {
-				err |= ERR_QUEUE_OVERFLOW;
+				put_camera_ray(W, out, pos, __float_as_int(ra.w), item, j);
 			}
 		}
 	}
+	// one atomic per warp: every lane of the block reaches this point
+	for (int o = 16; o > 0; o >>= 1) done += __shfl_down_sync(0xffffffffu, done, o);
+	if (lane_id() == 0 && done) atomicAdd(&W.stat[1], done);
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
+// The accumulate and generate steps on their own, for estimators whose
+// shading pass lists finished paths (ta/tb) for further use.
 __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 	const unsigned n = W.cnt[2];
 	const int out = par ^ 1;
@@ -220,33 +263,8 @@ __global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
 			slot = __float_as_int(a.w);
 			item = (int64_t)(unsigned)__float_as_int(b.x);
 			j = __float_as_int(b.y);
-			f3 L = ld3(a);
-			if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
-				err |= ERR_NONFINITE;
-				L = f3{ 0.f, 0.f, 0.f };
-			}
-			// Kahan accumulation of this path's radiance into the slot
-			float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
-			float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
-			float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
-			cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
-			sm = make_float4(ts[0], ts[1], ts[2], 0.f);
-			q = make_float4(q.x + L.x * L.x, q.y + L.y * L.y, q.z + L.z * L.z, 0.f);
 			++done;
-			++j;
-			int chunk_len = min(W.chunk, W.spp - (int)((uint32_t)item / (uint32_t)W.npix) * W.chunk);
-			if (j >= chunk_len) {
-				// item complete: publish its sums, take the next item
-				W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
-				W.item_q[item] = q;
-				sm = cm = q = make_float4(0.f, 0.f, 0.f, 0.f);
-				item = (int64_t)atomicAdd(&W.cnt[3], 1u);
-				j = 0;
-			}
-			W.acc_s[slot] = sm;
-			W.acc_c[slot] = cm;
-			W.acc_q[slot] = q;
-			emit = item < W.n_items;
+			emit = finish_path(W, slot, ld3(a), item, j, err, &W.cnt[3]);
 		}
 		unsigned pos = warp_append(&W.cnt[out], emit);
 		if (emit) {
@@ -435,7 +453,6 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 
 	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
-	const int g_gen = grid_for((const void *)k_generate, sc->n_sms);
 	const DevScene S = sc->dev;
 
 	unsigned init[8] = { (unsigned)std::min<int64_t>(P, W.n_items), 0u, 0u, (unsigned)std::min<int64_t>(P, W.n_items),
@@ -459,8 +476,6 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			cudaEventRecordWithFlags(kev[4 * it + 1], s, cudaEventRecordExternal);
 			k_shade<<<g_sh, BLOCK, 0, s>>>(S, W, par);
 			cudaEventRecordWithFlags(kev[4 * it + 2], s, cudaEventRecordExternal);
-			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
-			cudaEventRecordWithFlags(kev[4 * it + 3], s, cudaEventRecordExternal);
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
 	}
@@ -477,7 +492,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		++g;
 		iterations += GRAPH_ITERS;
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
-			for (int k = 0; k < 3; ++k) {
+			for (int k = 0; k < 2; ++k) {  // intersect; shade (with accumulate and generate)
 				float ms = 0.f;
 				if (cudaEventElapsedTime(&ms, kev[4 * it + k], kev[4 * it + k + 1]) == cudaSuccess) kms[k] += ms;
 				++launches[k];

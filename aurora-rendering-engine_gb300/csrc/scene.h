@@ -52,5 +52,9 @@ are_status batch_autotune(const are_scene_desc *const *descs, const are_camera *
 are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_params &p, float *rgb,
 	are_render_stats *stats);
 are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, int32_t device_ptrs, float *ms);
+are_status tonemap(const float *rgb, int64_t n, const are_tonemap_params *p, uint8_t *out);
+are_status write_ppm(const char *path, const uint8_t *rgb8, int w, int h);
+are_status write_pfm(const char *path, const float *rgb, int w, int h);
+are_status read_ppm(const char *path, int *w, int *h, float *texels);
 
 }  // namespace are_core

@@ -156,9 +156,11 @@ __device__ __forceinline__ Surface surface_at(const DevScene &S, int leaf, f3 o,
 
 // One bounce of the path estimator at depth `depth`.  Returns false if the
 // path ends here; on true, `nd` is the next direction and beta was updated.
-// L receives emission.
+// L receives emission.  Russian roulette survives with max(beta) * rr_scale
+// (capped at 1); rr_scale is 1 except on guided paths, where it removes the
+// guided bounces' pdf ratios from the survival probability.
 __device__ __forceinline__ bool scatter(const DevScene &S, const Surface &sf, f3 d, uint64_t key, int depth,
-	int rr_depth, f3 &beta, f3 &L, f3 &nd) {
+	int rr_depth, f3 &beta, f3 &L, f3 &nd, float rr_scale = 1.0f) {
 	float cosi = dot(d, sf.ng);
 	bool front = cosi < 0.0f;
 	f3 n = front ? sf.ng : scl(sf.ng, -1.0f);
@@ -212,7 +214,7 @@ __device__ __forceinline__ bool scatter(const DevScene &S, const Surface &sf, f3
 	}
 	if (rr_depth >= 0 && depth >= rr_depth) {
 		// rt.cpp:304-308, survival probability capped at 1
-		float q = fmaxf(fmaxf(beta.x, beta.y), beta.z);
+		float q = fmaxf(fmaxf(beta.x, beta.y), beta.z) * rr_scale;
 		if (q < 1.0f) {
 			if (uniform(key, cb + 3) >= q) return false;
 			beta = scl(beta, 1.0f / q);

@@ -47,12 +47,13 @@ WORKLOADS = {
     "cornell": (1, "cornell_box_600x600_1024spp_depth50"),
     "spheres": (0, "random_spheres_400x225_32spp_depth50"),
     "mesh": (2, "displaced_icosphere_2M_tris_1920x1080_256spp_depth16"),
+    "batch": (6, "uneven_batch_64_sphere_fields_50_to_200k_one_launch"),
 }
 WORKLOAD = WORKLOADS["cornell"][1]
-# algorithmic bytes of the wavefront's compulsory SoA traffic per path segment
-BYTES_INTERSECT = 32 + 16                    # ray record in, hit record out
-BYTES_SHADE = 32 + 16 + 32 + 32 + 32 + 4      # ray, hit, path state read + write, next ray, list index
-BYTES_GENERATE = 4 + 32 + 48 + 48 + 32 + 32   # list index, state read, accumulator read + write, state, camera ray
+# algorithmic bytes of the wavefront's compulsory SoA traffic
+BYTES_INTERSECT = 32 + 16          # per segment: ray (origin, direction) in, hit record out
+BYTES_SHADE_SEGMENT = 64 + 16 + 64  # per segment: queue record + hit in, one 64-byte record out (next ray or camera ray)
+BYTES_SHADE_SAMPLE = 48 + 48       # per sample: the slot's Kahan accumulators read and written
 
 
 def dist_env():
@@ -146,8 +147,10 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
     """Equal-time relMSE of guided vs plain rendering on the occluded-light
     Cornell box (200x200, depth 16) against the FP64 65,536-spp CPU reference
     in tests/golden/guiding_reference_200.npz.  Each method gets the same
-    wall-clock budget for one render (the guided one trains its network online
-    inside that budget, from a fresh random initialisation)."""
+    wall-clock budget for one render.  Two starts of the guided one:
+    "cold": a fresh random network that trains online inside the budget;
+    "warm": the network trained online during earlier renders of the scene
+    (as in progressive or animation rendering), training on inside the budget."""
     import numpy as np
 
     import are_gb300 as are
@@ -161,7 +164,7 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
     s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
     par = dict(par, width=res, height=res)
     sc = are.Scene(s)
-    gp = are.GuideParams.make(batch=1 << 16)
+    gp = are.GuideParams.make(guide_depth=3, batch=1 << 14, train=2)
 
     def relmse(img):
         return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
@@ -176,17 +179,117 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
     _, tp = timed(lambda: sc.render(cam, dict(par, spp=256, seed=91), with_var=False))
     spp_g = max(1, int(budget_s / (tg / 256)))
     spp_p = max(1, int(budget_s / (tp / 256)))
-    (gi, _, gst), t_g = timed(lambda: sc.render_guided(are.Guide(seed=1), cam, dict(par, spp=spp_g, seed=1), gp,
-                                                       with_var=False))
     (pi, _, _), t_p = timed(lambda: sc.render(cam, dict(par, spp=spp_p, seed=2), with_var=False))
-    eg, ep = relmse(gi), relmse(pi)
+    ep = relmse(pi)
+    out = {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]), "budget_s": budget_s,
+           "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)}}
+    g = are.Guide(seed=1)
+    (gi, _, gst), t_g = timed(lambda: sc.render_guided(g, cam, dict(par, spp=spp_g, seed=1), gp, with_var=False))
+    eg = relmse(gi)
+    out["guided_cold"] = {"spp": spp_g, "seconds": round(t_g, 3), "relmse": round(eg, 6),
+                          "adam_steps": gst["train_steps"], "relmse_plain_over_guided": round(ep / eg, 3)}
+    # warm start: the same network after six more 1024-spp renders of training
+    t = time.perf_counter()
+    for k in range(6):
+        sc.render_guided(g, cam, dict(par, spp=1024, seed=100 + k), gp, with_var=False)
+    t_train = time.perf_counter() - t
+    (gw, _, wst), t_w = timed(lambda: sc.render_guided(g, cam, dict(par, spp=spp_g, seed=3), gp, with_var=False))
+    ew = relmse(gw)
+    out["guided_warm"] = {"spp": spp_g, "seconds": round(t_w, 3), "relmse": round(ew, 6),
+                          "prior_training_s": round(t_train, 3), "adam_steps_total": len(g.loss_history()),
+                          "relmse_plain_over_guided": round(ep / ew, 3)}
+    out["relmse_plain_over_guided"] = out["guided_cold"]["relmse_plain_over_guided"]
     sc.close()
-    return {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]),
-            "budget_s": budget_s,
-            "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)},
-            "guided": {"spp": spp_g, "seconds": round(t_g, 3), "relmse": round(eg, 6),
-                       "adam_steps": gst["train_steps"]},
-            "relmse_plain_over_guided": round(ep / eg, 3)}
+    return out
+
+
+def run_batch(args, rank, world) -> None:
+    """--workload batch: 64 sphere-field scenes of uneven size (50 .. 200,000
+    spheres, 256x256 .. 1280x720, 16 .. 256 spp) in one persistent launch per
+    step, launch shape picked by the autotuner on a calibration run first."""
+    import numpy as np
+    import torch
+
+    import are_gb300 as are
+
+    import dataclasses
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    wl = are.batch_workload(n_scenes=64, seed=2026)
+    arrays = [a for a, _, _ in wl]
+    cams = [c for _, c, _ in wl]
+    params = [dict(p, seed=p["seed"] + 17 * rank) for _, _, p in wl]
+    t = time.perf_counter()
+    best, tuned_ms = are.batch_autotune(arrays, cams, params, calib_spp=2)
+    tune_s = time.perf_counter() - t
+    arrays = [dataclasses.replace(a, bvh_leaf_size=best.leaf_size) for a in arrays]
+    scenes = [are.Scene(a) for a in arrays]
+    samples_per_step = sum(p["width"] * p["height"] * p["spp"] for p in params)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for i in range(args.warmup):
+        are.render_batch(scenes, cams, [dict(p, seed=p["seed"] + 1000 + i) for p in params], best, want_images=False)
+    torch.cuda.synchronize()
+    stats, scene_ms = [], []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            _, ms, st = are.render_batch(scenes, cams, [dict(p, seed=p["seed"] + i) for p in params], best,
+                                         want_images=False)
+            stats.append(st)
+            scene_ms.append(ms)
+    dev_ms = sum(s["device_ms"] for s in stats)
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([dev_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = world * samples_per_step * args.steps / (dev_ms / 1e3) / 1e6
+    segments = sum(s["segments"] for s in stats)
+    # end to end: scenes built from host descriptors, one launch, images copied back, scenes freed
+    e2e_t = []
+    h2d = sum(sum(x.nbytes for x in a.__dict__.values() if hasattr(x, "nbytes")) for a in arrays)
+    d2h = sum(p["width"] * p["height"] * 12 for p in params)
+    for i in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc2 = [are.Scene(a) for a in arrays]
+        are.render_batch(sc2, cams, [dict(p, seed=p["seed"] + 50 + i) for p in params], best, want_images=True)
+        for x in sc2:
+            x.close()
+        e2e_t.append(time.perf_counter() - t0)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        big = max(range(len(arrays)), key=lambda k: arrays[k].n_prims)
+        r = cpu_sample(arrays[big], cams[big], params[big], float(os.environ.get("ARE_CPU_SECONDS", "15")),
+                       os.cpu_count() or 1)
+        cpu = {"value": round(r["value"], 4), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"largest scene ({arrays[big].n_prims} primitives): {r['rows']} rows x "
+                         f"{params[big]['width']} px x {r['spp']} spp ({r['seconds']:.1f} s)"}
+    last = np.array(scene_ms[-1])
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["batch"][1], "scenes": len(scenes),
+                       "primitives": [min(a.n_prims for a in arrays), max(a.n_prims for a in arrays)],
+                       "samples_per_step": samples_per_step, "parallelism": f"replicas{world}",
+                       "l2": "flushed (256 MB write) between steps"},
+            "autotuned": {**best.to_dict(), "calibration_ms": round(tuned_ms, 3), "tune_s": round(tune_s, 2)},
+            "scene_completion_ms": {"min": round(float(last.min()), 3), "median": round(float(np.median(last)), 3),
+                                    "max": round(float(last.max()), 3)},
+            "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
+            "e2e": {"value": round(samples_per_step / statistics.median(e2e_t) / 1e6 * world, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": None, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": sum(s["kernel_launches"]["other"] for s in stats),
+        }
+        print(json.dumps(line), flush=True)
+    for x in scenes:
+        x.close()
 
 
 def run_reference(args, rank, world) -> None:
@@ -247,6 +350,12 @@ def main() -> None:
             pg.destroy_process_group()
         return
 
+    if args.workload == "batch":
+        run_batch(args, rank, world)
+        if pg:
+            pg.destroy_process_group()
+        return
+
     import numpy as np
     import torch
 
@@ -296,9 +405,9 @@ def main() -> None:
     launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
     segments = sum(s["segments"] for s in stats)
     samples = sum(s["samples"] for s in stats)
-    algo = {"intersect": BYTES_INTERSECT * segments, "shade": BYTES_SHADE * segments,
-            "generate": BYTES_GENERATE * samples}
-    dom = max(("intersect", "shade", "generate"), key=lambda k: tot[k])
+    algo = {"intersect": BYTES_INTERSECT * segments,
+            "shade": BYTES_SHADE_SEGMENT * segments + BYTES_SHADE_SAMPLE * samples}
+    dom = max(("intersect", "shade"), key=lambda k: tot[k])
     peaks = measured_peaks()
     achieved = algo[dom] / (tot[dom] / 1e3) / 1e9
     roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",

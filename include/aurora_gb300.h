@@ -48,7 +48,8 @@ typedef enum are_status {
 	ARE_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
 	ARE_ERR_NO_DEVICE = 4,        /* no usable sm_103 device */
 	ARE_ERR_KERNEL_TIMEOUT = 5,   /* a bounded device-side wait gave up */
-	ARE_ERR_INTERNAL = 6          /* device error word set (queue overflow, bad index) */
+	ARE_ERR_INTERNAL = 6,         /* device error word set (queue overflow, bad index) */
+	ARE_ERR_IO = 7                /* an image file could not be opened, read or written */
 } are_status;
 
 /* ---- scene description (flat arrays, copied by are_scene_create) -------- */
@@ -255,6 +256,11 @@ ARE_API are_status are_guide_forward(are_guide *guide, const float *features, in
 /* samples: n x 13 host floats (features 9, direction 3, weight 1).  Mean loss
  * and its gradient (are_guide_param_count() floats), parameters unchanged. */
 ARE_API are_status are_guide_gradient(are_guide *guide, const float *samples, int64_t n, float *loss, float *grad);
+/* The mixture the renderer samples, n x 48 floats per row: lobe l's
+ * (mu.x, mu.y, mu.z, kappa) at 4 l and (weight pi_l, normaliser
+ * kappa / (2 pi (1 - e^-2 kappa))) at 32 + 2 l; the density of a unit
+ * direction w is sum_l pi_l norm_l exp(kappa_l (mu_l . w - 1)). */
+ARE_API are_status are_guide_mixture(are_guide *guide, const float *features, int64_t n, float *out);
 /* losses of the most recent Adam steps taken inside renders (oldest first);
  * returns how many were written (at most max) */
 ARE_API int32_t are_guide_loss_history(are_guide *guide, float *out, int32_t max);
@@ -264,8 +270,9 @@ ARE_API are_status are_guide_train(are_guide *guide, const float *samples, int64
 typedef struct are_guide_params {
 	float mix;            /* probability of drawing a guided vertex's direction from the network (one-sample MIS) */
 	int32_t guide_depth;  /* diffuse bounces guided per path: 0 .. 4 */
-	int32_t train;        /* train the network online during the render */
-	int32_t batch;        /* training samples per Adam step (e.g. 2^18) */
+	int32_t train;        /* Adam steps on each collected batch during the render (0 = network frozen, at most 16) */
+	int32_t batch;        /* training samples per Adam step (e.g. 2^18); a step is taken between
+	                         graph launches once a quarter batch has been collected */
 	float lr;             /* Adam learning rate */
 	float weight_clip;    /* cap on a sample's weight relative to the batch mean (0 = none) */
 	int32_t reserved_[2];
@@ -276,7 +283,8 @@ typedef struct are_guide_params {
  * network's mixture with probability mix, else by cosine sampling, and
  * weighted by the combined density, so the image stays unbiased whatever the
  * network has learned.  With train != 0 the network trains on the render's
- * own paths (stats->reserved_ returns the number of Adam steps taken). */
+ * own paths; stats->aux holds the training samples emitted, the Adam steps
+ * taken, the guided vertices and the last loss. */
 ARE_API are_status are_render_guided(are_scene *scene, are_guide *guide, const are_camera *camera,
 	const are_render_params *params, const are_guide_params *guide_params, float *rgb_out, float *var_out,
 	are_render_stats *stats);
@@ -308,6 +316,41 @@ ARE_API are_status are_render_batch(are_scene *const *scenes, const are_camera *
  * the scenes from their descriptors, and returns the fastest combination. */
 ARE_API are_status are_batch_autotune(const are_scene_desc *const *descs, const are_camera *cameras,
 	const are_render_params *params, int32_t n, int32_t calib_spp, are_batch_options *best, double *best_ms);
+
+/* ---- output formats ----------------------------------------------------- */
+
+typedef enum are_tonemap_mode {
+	/* Replaces writePPM's quantisation (experiments/rt.cpp:380-386): clamp to
+	 * [0,1] (NaN -> 1), powf(c, 1 / gamma) * 255 in FP32, truncated; gamma 2.2
+	 * there. */
+	ARE_TONEMAP_GAMMA = 0,
+	/* Replaces are::Texture::save_texture's quantisation (src/texture.cpp:378-383):
+	 * clamp(c * 255.0, 0, 255) in FP64, truncated (NaN -> 0, undefined there). */
+	ARE_TONEMAP_LINEAR = 1
+} are_tonemap_mode;
+
+typedef struct are_tonemap_params {
+	int32_t mode;       /* are_tonemap_mode */
+	float gamma;        /* ARE_TONEMAP_GAMMA: 0.1 .. 10 */
+	uint32_t flags;     /* ARE_FLAG_DEVICE_OUTPUT: rgb and out are device pointers of the current device */
+	int32_t reserved_;
+} are_tonemap_params;
+
+/* n_values FP32 linear values (pixels x 3) -> bytes on the GPU, byte-identical
+ * to the reference formula of the mode for every input.  Host pointers are
+ * staged through a device buffer; device pointers are used in place.  Runs on
+ * the calling thread's default stream and returns when the bytes are written. */
+ARE_API are_status are_tonemap(const float *rgb, int64_t n_values, const are_tonemap_params *params, uint8_t *out);
+/* Replaces writePPM's file output (rt.cpp:377-392) and save_texture's
+ * (texture.cpp:362-395): "P6\n<w> <h>\n255\n" then the RGB bytes, top row first. */
+ARE_API are_status are_write_ppm(const char *path, const uint8_t *rgb8, int32_t width, int32_t height);
+/* FP32 RGB Portable Float Map (no reference counterpart: the linear image
+ * before quantisation), little-endian, bottom row first as the format wants. */
+ARE_API are_status are_write_pfm(const char *path, const float *rgb, int32_t width, int32_t height);
+/* Replaces are::Texture's PPM constructor (src/texture.cpp:9-50): a P6 file
+ * with maximum 255 -> width, height and, if texels is not null, width x height
+ * RGB floats byte / 255.0 in file order, ready for are_scene_desc.texels. */
+ARE_API are_status are_read_ppm(const char *path, int32_t *width, int32_t *height, float *texels);
 
 /* ---- synthetic workloads ------------------------------------------------ */
 

@@ -136,6 +136,7 @@ void orc_hemisphere_f32(const float *n, float u, float v, float *dir); /* rt.cpp
 void orc_reflect_f64(const double *v, const double *n, double *out);
 void orc_refract_f64(const double *uv, const double *n, double eta, double *out);
 void orc_ppm_quantize(const float *rgb, int64_t n, float gamma, uint8_t *out); /* rt.cpp:384-386 */
+void orc_texture_quantize(const float *rgb, int64_t n, uint8_t *out);          /* texture.cpp:378-383 */
 
 /* The reference's own estimator, rt.cpp trace()/computeAO() (rt.cpp:221-374).
  * rng_mode 1: rt.cpp's per-row std::mt19937 seeded mt_seed + y; rng_mode 0:

@@ -149,6 +149,7 @@ class Oracle:
         L.orc_reflect_f64.argtypes = [_d, _d, _d]
         L.orc_refract_f64.argtypes = [_d, _d, C.c_double, _d]
         L.orc_ppm_quantize.argtypes = [_f, C.c_int64, C.c_float, C.POINTER(C.c_uint8)]
+        L.orc_texture_quantize.argtypes = [_f, C.c_int64, C.POINTER(C.c_uint8)]
         L.orc_render_legacy.argtypes = [C.c_void_p, C.POINTER(OrcCamera), C.POINTER(OrcParams), _f, C.c_int32,
                                         C.c_uint32, C.c_int32]
         L.orc_mt19937.argtypes = [C.c_uint32, C.c_int64, C.POINTER(C.c_uint32), _f]
@@ -162,6 +163,17 @@ class Oracle:
         self.lib = L
 
     # path-guiding network (FP64) -------------------------------------------------
+    def quantize(self, rgb: np.ndarray, mode: int = 0, gamma: float = 2.2) -> np.ndarray:
+        """8-bit quantisation: mode 0 rt.cpp:384-386 (gamma), 1 texture.cpp:378-383 (linear)."""
+        a = np.ascontiguousarray(rgb, np.float32).reshape(-1)
+        out = np.empty(a.size, np.uint8)
+        u8 = out.ctypes.data_as(C.POINTER(C.c_uint8))
+        if mode == 0:
+            self.lib.orc_ppm_quantize(a.ctypes.data_as(_f), a.size, gamma, u8)
+        else:
+            self.lib.orc_texture_quantize(a.ctypes.data_as(_f), a.size, u8)
+        return out.reshape(np.shape(rgb))
+
     def guide_forward(self, params: np.ndarray, feat: np.ndarray) -> np.ndarray:
         params = np.ascontiguousarray(params, np.float32)
         feat = np.ascontiguousarray(feat, np.float32).reshape(-1, 9)

@@ -184,6 +184,18 @@ void orc_refract_f64(const double *uv, const double *n, double eta, double *out)
 
 /* writePPM quantisation, rt.cpp:377-392: clamp to [0,1], pow(c, 1/gamma),
  * times 255, truncate to unsigned char. */
+/* are::Texture::save_texture (src/texture.cpp:378-383): the FP64 image value
+ * times 255.0, clamped to [0, 255], truncated.  The image is FP32 here, so
+ * the product is exact; NaN (undefined in the reference) gives 0. */
+void orc_texture_quantize(const float *rgb, int64_t n, uint8_t *out) {
+	for (int64_t i = 0; i < n; ++i) {
+		double v = (double)rgb[i] * 255.0;
+		if (v != v) v = 0.0;
+		v = v < 0.0 ? 0.0 : (v > 255.0 ? 255.0 : v);
+		out[i] = (uint8_t)v;
+	}
+}
+
 void orc_ppm_quantize(const float *rgb, int64_t n, float gamma, uint8_t *out) {
 	for (int64_t i = 0; i < n; ++i) {
 		float c = rgb[i];

@@ -134,3 +134,23 @@ def test_device_training_learns_a_direction_field(gpu_lib, oracle):
     after = np.mean([np.log(oracle.guide_pdf(o, w)) for o, w in zip(oracle.guide_forward(p1, test[:, :9]), truth)])
     assert losses[-1] < losses[0] - 1.0, (losses[0], losses[-1])
     assert after > before + 2.0, (before, after)  # density at the true direction up by > e^2
+
+
+@pytest.mark.gpu
+def test_device_mixture_density_matches_oracle(gpu_lib, oracle):
+    """The packed mixture the renderer samples gives the oracle's density."""
+    rng = np.random.Generator(np.random.PCG64(17))
+    g = are.Guide(seed=9)
+    p = g.params
+    feat = rng.uniform(-1, 1, (300, 9)).astype(np.float32)
+    mix = g.mixture(feat)
+    raw = oracle.guide_forward(p, feat)
+    w = rng.normal(size=(300, 3))
+    w /= np.linalg.norm(w, axis=1, keepdims=True)
+    for m, o, d in zip(mix, raw, w):
+        mu, kappa = m[:32].reshape(8, 4)[:, :3], m[:32].reshape(8, 4)[:, 3]
+        pi, nrm = m[32:].reshape(8, 2)[:, 0], m[32:].reshape(8, 2)[:, 1]
+        assert abs(pi.sum() - 1) < 1e-5 and np.allclose(np.linalg.norm(mu, axis=1), 1, atol=1e-6)
+        q = float(np.sum(pi * nrm * np.exp(kappa * (mu @ d - 1))))
+        r = oracle.guide_pdf(o, d)
+        assert abs(q - r) <= 0.03 * r + 1e-4, (q, r)
