@@ -48,6 +48,7 @@ WORKLOADS = {
     "spheres": (0, "random_spheres_400x225_32spp_depth50"),
     "mesh": (2, "displaced_icosphere_2M_tris_1920x1080_256spp_depth16"),
     "batch": (6, "uneven_batch_64_sphere_fields_50_to_200k_one_launch"),
+    "guided": (4, "cornell_occluded_600x600_1024spp_depth16_guided"),
 }
 WORKLOAD = WORKLOADS["cornell"][1]
 # algorithmic bytes of the wavefront's compulsory SoA traffic
@@ -108,6 +109,26 @@ class ClockSampler:
         loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
         return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+def barrier(world: int) -> None:
+    """All ranks meet (gloo) before and after a timed region; no-op at N = 1."""
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """The slowest rank's figure (gloo all-reduce of one float64)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def measured_peaks() -> dict:
@@ -230,6 +251,8 @@ def run_batch(args, rank, world) -> None:
     for i in range(args.warmup):
         are.render_batch(scenes, cams, [dict(p, seed=p["seed"] + 1000 + i) for p in params], best, want_images=False)
     torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
     stats, scene_ms = [], []
     with ClockSampler(local) as clk:
         for i in range(args.steps):
@@ -239,13 +262,9 @@ def run_batch(args, rank, world) -> None:
                                          want_images=False)
             stats.append(st)
             scene_ms.append(ms)
-    dev_ms = sum(s["device_ms"] for s in stats)
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([dev_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms = float(tt.item())
+    torch.cuda.synchronize()
+    barrier(world)
+    dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
     value = world * samples_per_step * args.steps / (dev_ms / 1e3) / 1e6
     segments = sum(s["segments"] for s in stats)
     # end to end: scenes built from host descriptors, one launch, images copied back, scenes freed
@@ -290,6 +309,60 @@ def run_batch(args, rank, world) -> None:
         print(json.dumps(line), flush=True)
     for x in scenes:
         x.close()
+
+
+def run_guided(args, rank, world) -> None:
+    """--workload guided: the occluded-light Cornell frame (600x600, 1024 spp,
+    depth 16) through are_render_guided, the network training online from a
+    fresh initialisation during the warm-up frames and on through the timed
+    ones (guide depth 3, batch 2^14, two Adam steps per batch)."""
+    import torch
+
+    import are_gb300 as are
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cfg_id, workload = WORKLOADS["guided"]
+    scene_arrays, cam, par = are.build_config(cfg_id)
+    spp = args.spp if args.spp > 0 else par["spp"]
+    par = dict(par, spp=spp)
+    W, H = par["width"], par["height"]
+    sc = are.Scene(scene_arrays)
+    g = are.Guide(seed=1 + rank)
+    gp = are.GuideParams.make(guide_depth=3, batch=1 << 14, train=2)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for i in range(args.warmup):
+        sc.render_guided(g, cam, dict(par, seed=1000 + i), gp, with_var=False)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    stats = []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            stats.append(sc.render_guided(g, cam, dict(par, seed=1 + i), gp, with_var=False)[2])
+    torch.cuda.synchronize()
+    barrier(world)
+    dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
+    samples = W * H * spp
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(world * samples * args.steps / (dev_ms / 1e3) / 1e6, 3), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f16 network",
+            "data": "synthetic",
+            "config": {"workload": workload, "width": W, "height": H, "spp": spp, "max_depth": par["max_depth"],
+                       "guide_depth": 3, "mix": 0.5, "train_batch": 1 << 14, "parallelism": f"replicas{world}",
+                       "l2": "flushed (256 MB write) between steps"},
+            "adam_steps_per_frame": round(sum(s["train_steps"] for s in stats) / len(stats), 1),
+            "guided_vertices_per_sample": round(sum(s["guided_vertices"] for s in stats) / (samples * len(stats)), 3),
+            "segments_per_sample": round(sum(s["segments"] for s in stats) / (samples * len(stats)), 4),
+            "clocks": clk.summary(),
+            "gpu_launches": sum(sum(s["kernel_launches"].values()) for s in stats),
+        }
+        print(json.dumps(line), flush=True)
+    sc.close()
 
 
 def run_reference(args, rank, world) -> None:
@@ -350,8 +423,8 @@ def main() -> None:
             pg.destroy_process_group()
         return
 
-    if args.workload == "batch":
-        run_batch(args, rank, world)
+    if args.workload in ("batch", "guided"):
+        (run_batch if args.workload == "batch" else run_guided)(args, rank, world)
         if pg:
             pg.destroy_process_group()
         return
@@ -391,12 +464,8 @@ def main() -> None:
             stats.append(step(1 + i))
         torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
-    dev_ms = sum(s["device_ms"] for s in stats)
-    if pg:
-        t = torch.tensor([dev_ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dev_ms = float(t.item())
-        pg.barrier()
+    barrier(world)
+    dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
     torch.cuda.synchronize()
     value = world * samples_per_step * args.steps / (dev_ms / 1e3) / 1e6
 
