@@ -28,6 +28,7 @@ TEX_SOLID, TEX_CHECKER, TEX_IMAGE = 0, 1, 2
 MAP_SURFACE_UV, MAP_SPHERICAL = 0, 1
 BG_CONSTANT, BG_SKY_GRADIENT = 0, 1
 TRI_REFERENCE_MT, TRI_WATERTIGHT = 0, 1
+BVH_HOST_SAH, BVH_DEVICE = 0, 1
 EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
 FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
@@ -72,6 +73,7 @@ class SceneArrays:
     bg_b: tuple = (0.0, 0.0, 0.0)
     triangle_test: int = TRI_WATERTIGHT
     bvh_leaf_size: int = 0
+    bvh_build: int = 0
 
     @property
     def n_prims(self) -> int:
@@ -134,7 +136,7 @@ class SceneDesc(C.Structure):
         ("n_textures", C.c_int32), ("textures", C.c_void_p),
         ("n_texels", C.c_int64), ("texels", _f),
         ("background", C.c_int32), ("bg_a", C.c_float * 3), ("bg_b", C.c_float * 3),
-        ("triangle_test", C.c_int32), ("bvh_leaf_size", C.c_int32),
+        ("triangle_test", C.c_int32), ("bvh_leaf_size", C.c_int32), ("bvh_build", C.c_int32),
     ]
 
 
@@ -250,6 +252,7 @@ def desc_struct(s: SceneArrays) -> tuple[SceneDesc, list]:
     d.bg_b = (C.c_float * 3)(*[float(v) for v in s.bg_b])
     d.triangle_test = int(s.triangle_test)
     d.bvh_leaf_size = int(s.bvh_leaf_size)
+    d.bvh_build = int(s.bvh_build)
     return d, keep
 
 
@@ -276,7 +279,7 @@ def arrays_from_desc(d: SceneDesc) -> SceneArrays:
         s.textures = np.frombuffer(bytes(buf), TEXTURE_DTYPE).copy()
     s.texels = _copy(d.texels, d.n_texels, 3) if d.n_texels else None
     s.background, s.bg_a, s.bg_b = d.background, tuple(d.bg_a), tuple(d.bg_b)
-    s.triangle_test, s.bvh_leaf_size = d.triangle_test, d.bvh_leaf_size
+    s.triangle_test, s.bvh_leaf_size, s.bvh_build = d.triangle_test, d.bvh_leaf_size, d.bvh_build
     return s
 
 

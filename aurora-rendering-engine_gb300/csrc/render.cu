@@ -176,6 +176,74 @@ __device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64
 	return item < W.n_items;
 }
 
+// A path between bounces: its ray and the state that travels with it.
+struct PathState {
+	f3 o, d, beta, L;
+	int slot, depth, j;
+	int64_t item;
+};
+
+__device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i) {
+	const float4 ra = W.qa[q][i], rb = W.qb[q][i], rc = W.qc[q][i], rd = W.qd[q][i];
+	PathState P;
+	P.o = ld3(ra), P.d = ld3(rb), P.beta = ld3(rc), P.L = ld3(rd);
+	P.slot = __float_as_int(ra.w);
+	const int meta = __float_as_int(rb.w);
+	P.depth = meta & 0xff, P.j = meta >> 8;
+	P.item = (int64_t)(unsigned)__float_as_int(rc.w);
+	return P;
+}
+
+__device__ __forceinline__ void store_path(const Wave &W, int q, unsigned pos, const PathState &P) {
+	W.qa[q][pos] = make_float4(P.o.x, P.o.y, P.o.z, __int_as_float(P.slot));
+	W.qb[q][pos] = make_float4(P.d.x, P.d.y, P.d.z, __int_as_float(P.depth | (P.j << 8)));
+	W.qc[q][pos] = make_float4(P.beta.x, P.beta.y, P.beta.z, __int_as_float((int)P.item));
+	W.qd[q][pos] = make_float4(P.L.x, P.L.y, P.L.z, 0.f);
+}
+
+// The first ray of sample j of work item `item`, as put_camera_ray writes it.
+__device__ __forceinline__ void camera_path(const Wave &W, int slot, int64_t item, int j, PathState &P) {
+	int pixel, sample;
+	item_coords(W, item, j, pixel, sample);
+	uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+	camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, P.o, P.d);
+	P.beta = f3{ 1.f, 1.f, 1.f };
+	P.L = f3{ 0.f, 0.f, 0.f };
+	P.slot = slot, P.depth = 0, P.j = j, P.item = item;
+}
+
+// One bounce of path P at hit h (t, leaf bits, u, v): scatter and, when the
+// path ends, the accumulate step and the slot's next camera path.  Returns
+// true if P holds a ray to trace (the continued path or the new one).
+__device__ __forceinline__ bool shade_step(const DevScene &S, const Wave &W, PathState &P, float4 h, uint32_t &err,
+	unsigned long long &done) {
+	bool cont = false;
+	const int leaf = __float_as_int(h.y);
+	if (leaf < 0) {
+		P.L = add(P.L, mulv(P.beta, background(S, P.d)));
+	} else {
+		int pixel, sample;
+		item_coords(W, P.item, P.j, pixel, sample);
+		uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+		Surface sf = surface_at(S, leaf, P.o, P.d, h.x, h.z, h.w);
+		f3 nd;
+		cont = scatter(S, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd);
+		if (cont && P.depth + 1 >= W.max_depth) cont = false;
+		if (cont) {
+			P.o = sf.p;
+			P.d = nd;
+			++P.depth;
+			return true;
+		}
+	}
+	++done;
+	int64_t item = P.item;
+	int j = P.j;
+	if (!finish_path(W, P.slot, P.L, item, j, err, &W.cnt[3])) return false;
+	camera_path(W, P.slot, item, j, P);
+	return true;
+}
+
 // One bounce of every queued path, fused with the accumulate and generate
 // steps: a path that continues is appended to the next queue; a path that
 // ends adds its radiance to its slot (finish_path) and, if the slot has a
@@ -188,60 +256,65 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 	unsigned long long done = 0;
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		unsigned i = base + threadIdx.x;
-		bool valid = i < n;
-		bool cont = false, spawn = false;
-		f3 p, nd, beta, L;
-		float4 ra, rb, rc;
-		int64_t item = 0;
-		int j = 0;
-		if (valid) {
-			ra = W.qa[par][i];
-			rb = W.qb[par][i];
-			rc = W.qc[par][i];
-			float4 rd = W.qd[par][i];
-			float4 h = W.hit[i];
-			beta = ld3(rc);
-			L = ld3(rd);
-			int meta = __float_as_int(rb.w);
-			int depth = meta & 0xff;
-			j = meta >> 8;
-			item = (int64_t)(unsigned)__float_as_int(rc.w);
-			f3 o = ld3(ra), d = ld3(rb);
-			int leaf = __float_as_int(h.y);
-			if (leaf < 0) {
-				L = add(L, mulv(beta, background(S, d)));
-			} else {
-				int pixel, sample;
-				item_coords(W, item, j, pixel, sample);
-				uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
-				Surface sf = surface_at(S, leaf, o, d, h.x, h.z, h.w);
-				cont = scatter(S, sf, d, key, depth, W.rr_depth, beta, L, nd);
-				if (cont && depth + 1 >= W.max_depth) cont = false;
-				p = sf.p;
-			}
-			if (!cont) {
-				++done;
-				spawn = finish_path(W, __float_as_int(ra.w), L, item, j, err, &W.cnt[3]);
-			}
+		bool live = false;
+		PathState P;
+		if (i < n) {
+			P = load_path(W, par, i);
+			live = shade_step(S, W, P, W.hit[i], err, done);
 		}
-		unsigned pos = warp_append(&W.cnt[out], cont || spawn);
-		if (cont || spawn) {
-			if (pos >= (unsigned)W.P) {
+		unsigned pos = warp_append(&W.cnt[out], live);
+		if (live) {
+			if (pos < (unsigned)W.P)
+				store_path(W, out, pos, P);
+			else
 				err |= ERR_QUEUE_OVERFLOW;
-			} else if (cont) {
-				int meta = __float_as_int(rb.w) + 1;  // depth + 1, same sample
-				W.qa[out][pos] = make_float4(p.x, p.y, p.z, ra.w);
-				W.qb[out][pos] = make_float4(nd.x, nd.y, nd.z, __int_as_float(meta));
-				W.qc[out][pos] = make_float4(beta.x, beta.y, beta.z, rc.w);
-				W.qd[out][pos] = make_float4(L.x, L.y, L.z, 0.f);
-			} else {
-				put_camera_ray(W, out, pos, __float_as_int(ra.w), item, j);
-			}
 		}
 	}
 	// one atomic per warp: every lane of the block reaches this point
 	for (int o = 16; o > 0; o >>= 1) done += __shfl_down_sync(0xffffffffu, done, o);
 	if (lane_id() == 0 && done) atomicAdd(&W.stat[1], done);
+	if (err) atomicOr(&W.cnt[4], err);
+}
+
+// The end of a render, when every work item has been taken and few paths are
+// left: one thread per queued path traces it to the end, then the rest of
+// its slot's samples, with the same device functions and in the same sample
+// order as the wavefront, so the image is the same bit for bit.  It replaces
+// the long tail of nearly empty wavefront iterations (paths that keep
+// bouncing between glass and metal).
+__global__ void __launch_bounds__(BLOCK) k_tail(DevScene S, Wave W, int par) {
+	__shared__ float4 snodes[2 * SMEM_NODES];
+	int n_snodes = 0;
+	const unsigned n = W.cnt[par];
+	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
+	const bool linear = S.n_prims <= LINEAR_MAX;
+	if (linear) {
+		stage_prims(S, snodes);
+		__syncthreads();
+	} else {
+		stage_nodes(S, snodes, n_snodes);
+	}
+	uint32_t err = 0;
+	unsigned long long done = 0, segments = 0;
+	const float inf = __int_as_float(0x7f800000);
+	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		PathState P = load_path(W, par, i);
+		bool live = true;
+		while (live) {
+			Hit hh = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf)
+							: closest_hit(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err);
+			++segments;
+			live = shade_step(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done);
+		}
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		done += __shfl_down_sync(0xffffffffu, done, o);
+		segments += __shfl_down_sync(0xffffffffu, segments, o);
+	}
+	if (lane_id() == 0) {
+		if (done) atomicAdd(&W.stat[1], done);
+		if (segments) atomicAdd(&W.stat[0], segments), atomicAdd(&W.stat[2], segments);
+	}
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
@@ -453,6 +526,8 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 
 	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
+	const int g_tail = grid_for((const void *)k_tail, sc->n_sms);
+	const unsigned tail_max = (unsigned)std::max<int64_t>(8192, P / 16);  // queued paths below which the tail runs
 	const DevScene S = sc->dev;
 
 	unsigned init[8] = { (unsigned)std::min<int64_t>(P, W.n_items), 0u, 0u, (unsigned)std::min<int64_t>(P, W.n_items),
@@ -499,6 +574,18 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			}
 		}
 		if (sc->host_counters[0] == 0) break;  // next iteration's input queue is empty
+		if (sc->host_counters[3] >= W.n_items && sc->host_counters[0] <= tail_max) {
+			// every work item is taken and few paths are left: finish them in one launch
+			cudaEventRecord(kev[0], s);
+			k_tail<<<g_tail, BLOCK, 0, s>>>(S, W, 0);
+			cudaEventRecord(kev[1], s);
+			st = cuda_status(cudaGetLastError(), "k_tail launch");
+			if (!st) st = cuda_status(cudaStreamSynchronize(s), "render tail");
+			float ms = 0.f;
+			if (!st && cudaEventElapsedTime(&ms, kev[0], kev[1]) == cudaSuccess) kms[ARE_KERNEL_OTHER] += ms;
+			++launches[ARE_KERNEL_OTHER];
+			break;
+		}
 		if (g > max_launches) {
 			set_error("render did not converge");
 			st = ARE_ERR_INTERNAL;
@@ -512,7 +599,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		st = cuda_status(cudaGetLastError(), "k_resolve launch");
 	}
 	cudaEventRecord(ev1, s);
-	unsigned long long hstat[2] = { 0, 0 };
+	unsigned long long hstat[3] = { 0, 0, 0 };
 	unsigned herr = 0;
 	if (!st) {
 		cudaMemcpyAsync(hstat, W.stat, sizeof hstat, cudaMemcpyDeviceToHost, s);
@@ -541,6 +628,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		stats->device_ms = total_ms;
 		for (int k = 0; k < 4; ++k) stats->kernel_ms[k] = kms[k], stats->kernel_launches[k] = launches[k];
 		stats->error_word = (int32_t)herr;
+		stats->aux[0] = (double)hstat[2];  // segments traced by the tail kernel (kernel_ms[ARE_KERNEL_OTHER])
 	}
 	return st;
 }

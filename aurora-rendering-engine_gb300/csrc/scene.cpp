@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "bvh.h"
+#include "lbvh.h"
 #include "scene.h"
 
 namespace are_core {
@@ -58,6 +59,7 @@ are_status validate(const are_scene_desc *d) {
 	int64_t total = (int64_t)d->n_spheres + d->n_quads + d->n_triangles;
 	if (total > (int64_t)INT32_MAX / 4) return invalid("too many primitives");
 	if (d->background != ARE_BG_CONSTANT && d->background != ARE_BG_SKY_GRADIENT) return invalid("unknown background");
+	if (d->bvh_build != ARE_BVH_HOST_SAH && d->bvh_build != ARE_BVH_DEVICE) return invalid("unknown bvh_build");
 	if (d->triangle_test != ARE_TRI_REFERENCE_MT && d->triangle_test != ARE_TRI_WATERTIGHT)
 		return invalid("unknown triangle test");
 	for (int32_t i = 0; i < d->n_textures; ++i) {
@@ -132,6 +134,99 @@ are_status upload(are_scene *sc, const T *src, size_t count, const T **dst) {
 
 }  // namespace
 
+namespace {
+
+// record j of the descriptor in the DevScene layout (3 float4), input order
+void pack_record(const are_scene_desc *d, int32_t g, float *o, int32_t &mat) {
+	const int32_t ns = d->n_spheres, nq = d->n_quads;
+	std::memset(o, 0, 48);
+	if (g < ns) {
+		std::memcpy(o, d->spheres + 4 * (size_t)g, 16);
+		mat = d->sphere_mat[g];
+	} else if (g < ns + nq) {
+		const float *q = d->quads + 9 * (size_t)(g - ns);
+		for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, q + 3 * r, 12);
+		o[3] = PRIM_TAG_QUAD;
+		mat = d->quad_mat[g - ns];
+	} else {
+		const float *t = d->triangles + 9 * (size_t)(g - ns - nq);
+		for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, t + 3 * r, 12);
+		o[3] = PRIM_TAG_TRI;
+		mat = d->triangle_mat[g - ns - nq];
+	}
+}
+
+// The scene with its BVH built on the device: records are packed on the host
+// in input order (one pass), uploaded, and sorted into leaf order there.
+are_status scene_create_device(const are_scene_desc *d, are_scene **out) {
+	const int32_t ns = d->n_spheres, nq = d->n_quads, nt = d->n_triangles;
+	const int32_t n = ns + nq + nt;
+	std::vector<float> rec(12 * (size_t)n);
+	std::vector<int32_t> mat((size_t)n);
+	for (int32_t g = 0; g < n; ++g) pack_record(d, g, &rec[12 * (size_t)g], mat[g]);
+	std::vector<float> uv;
+	if (d->triangle_uv && nt) {
+		uv.assign(6 * (size_t)n, 0.0f);
+		std::memcpy(&uv[6 * (size_t)(ns + nq)], d->triangle_uv, 24 * (size_t)nt);
+	}
+	are_scene *sc = new are_scene();
+	cudaGetDevice(&sc->device);
+	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
+	are_status st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	void *tmp = nullptr;
+	const size_t rec_b = ((48 * (size_t)n + 255) & ~(size_t)255), mat_b = ((4 * (size_t)n + 255) & ~(size_t)255);
+	if (!st) st = cuda_status(cudaMalloc(&tmp, rec_b + mat_b + 24 * uv.size() / 6), "cudaMalloc(scene upload)");
+	LbvhResult r;
+	if (!st) {
+		char *z = (char *)tmp;
+		const float4 *d_rec = (const float4 *)z;
+		const int32_t *d_mat = (const int32_t *)(z + rec_b);
+		const float *d_uv = uv.empty() ? nullptr : (const float *)(z + rec_b + mat_b);
+		cudaMemcpyAsync(z, rec.data(), 48 * (size_t)n, cudaMemcpyHostToDevice, sc->stream);
+		cudaMemcpyAsync(z + rec_b, mat.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, sc->stream);
+		if (d_uv) cudaMemcpyAsync(z + rec_b + mat_b, uv.data(), 4 * uv.size(), cudaMemcpyHostToDevice, sc->stream);
+		st = build_bvh_device(sc, d_rec, d_mat, d_uv, n, d->bvh_leaf_size, r, sc->stream);
+	}
+	if (tmp) {
+		cudaStreamSynchronize(sc->stream);
+		cudaFree(tmp);
+	}
+	DevScene &S = sc->dev;
+	if (!st) st = upload(sc, (const DevMaterial *)d->materials, (size_t)d->n_materials, &S.mats);
+	if (!st) st = upload(sc, (const DevTexture *)d->textures, (size_t)d->n_textures, &S.texs);
+	if (!st) st = upload(sc, d->texels, 3 * (size_t)d->n_texels, &S.texels);
+	if (!st) st = cuda_status(cudaMallocHost((void **)&sc->host_counters, 64 * sizeof(unsigned)), "cudaMallocHost");
+	if (st) {
+		delete sc;
+		return st;
+	}
+	S.prims = r.prims;
+	S.prim_gid = r.gid;
+	S.prim_mat = r.mat;
+	S.tri_uv = r.uv;
+	S.nodes = r.nodes;
+	S.leaves = nullptr;
+	S.n_leaves = 0;
+	S.n_prims = n;
+	S.n_nodes = (int32_t)r.n_nodes;
+	S.n_materials = d->n_materials;
+	S.n_textures = d->n_textures;
+	S.background = d->background;
+	S.triangle_test = d->triangle_test;
+	for (int k = 0; k < 3; ++k) S.bg_a[k] = d->bg_a[k], S.bg_b[k] = d->bg_b[k];
+	S.box_pad = r.box_pad;
+	sc->n_prims = n;
+	sc->n_spheres = ns, sc->n_quads = nq, sc->n_triangles = nt;
+	for (int k = 0; k < 3; ++k) sc->box_lo[k] = r.lo[k], sc->box_hi[k] = r.hi[k];
+	sc->n_nodes = r.n_nodes;
+	sc->max_leaf = r.max_leaf;
+	sc->depth = r.depth;
+	*out = sc;
+	return ARE_OK;
+}
+
+}  // namespace
+
 are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	if (!out) return invalid("output handle pointer is null");
 	*out = nullptr;
@@ -144,6 +239,7 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	}
 	const int32_t ns = d->n_spheres, nq = d->n_quads, nt = d->n_triangles;
 	const int32_t n = ns + nq + nt;
+	if (d->bvh_build == ARE_BVH_DEVICE && n > LINEAR_MAX) return scene_create_device(d, out);
 
 	// primitive bounds in double
 	std::vector<PrimBox> boxes((size_t)n);

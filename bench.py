@@ -408,6 +408,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-guiding", action="store_true", help="skip the guided-vs-plain relMSE comparison")
     ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
+    ap.add_argument("--bvh", default="host", choices=["host", "device"],
+                    help="where scenes build their BVH: host binned SAH or the device LBVH")
     args = ap.parse_args()
     rank, world, local = dist_env()
     pg = None
@@ -438,6 +440,9 @@ def main() -> None:
     L = are.load()
     cfg_id, workload = WORKLOADS[args.workload]
     scene_arrays, cam, par = are.build_config(cfg_id)
+    import dataclasses
+
+    scene_arrays = dataclasses.replace(scene_arrays, bvh_build=are.BVH_DEVICE if args.bvh == "device" else are.BVH_HOST_SAH)
     spp = args.spp if args.spp > 0 else par["spp"]
     par = dict(par, spp=spp, pool_size=args.pool, chunk=args.chunk)
     W, H = par["width"], par["height"]
@@ -474,8 +479,10 @@ def main() -> None:
     launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
     segments = sum(s["segments"] for s in stats)
     samples = sum(s["samples"] for s in stats)
-    algo = {"intersect": BYTES_INTERSECT * segments,
-            "shade": BYTES_SHADE_SEGMENT * segments + BYTES_SHADE_SAMPLE * samples}
+    tail_segments = sum(int(s["aux"][0]) for s in stats)  # traced by the end-of-render tail kernel ("other")
+    wave_segments = segments - tail_segments
+    algo = {"intersect": BYTES_INTERSECT * wave_segments,
+            "shade": BYTES_SHADE_SEGMENT * wave_segments + BYTES_SHADE_SAMPLE * samples}
     dom = max(("intersect", "shade"), key=lambda k: tot[k])
     peaks = measured_peaks()
     achieved = algo[dom] / (tot[dom] / 1e3) / 1e9
@@ -496,11 +503,13 @@ def main() -> None:
     import ctypes as C
 
     cam_s = are.Camera.from_dict(cam)
+    build_s = []
     for i in range(max(2, min(args.steps, 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h = C.c_void_p()
         are.check(L.are_scene_create(C.byref(d), C.byref(h)))
+        build_s.append(time.perf_counter() - t0)
         p = are.RenderParams.from_dict(dict(par, seed=77 + i))
         st = are.RenderStats()
         are.check(L.are_render(h, C.byref(cam_s), C.byref(p), host_rgb.ctypes.data, None, C.byref(st)))
@@ -508,7 +517,8 @@ def main() -> None:
         e2e_times.append(time.perf_counter() - t0)
     h2d = sum(a.nbytes for a in keep if hasattr(a, "nbytes"))
     e2e = {"value": round(samples_per_step / statistics.median(e2e_times) / 1e6 * world, 3), "unit": UNIT,
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.nbytes)}
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.nbytes),
+           "scene_create_ms": round(1e3 * statistics.median(build_s), 2)}
 
     guiding = None
     if rank == 0 and args.workload == "cornell" and not args.no_guiding:
@@ -528,9 +538,11 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
-                       "rr_depth": par["rr_depth"], "primitives": scene_arrays.n_prims, "parallelism": f"replicas{world}",
+                       "rr_depth": par["rr_depth"], "primitives": scene_arrays.n_prims, "bvh_build": args.bvh,
+                       "parallelism": f"replicas{world}",
                        "l2": "flushed (256 MB write) between steps; path pool > L2"},
             "segments_per_sample": round(segments / max(1, samples), 4),
+            "tail_segments_frac": round(tail_segments / max(1, segments), 5),
             "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
             "wall_s": round(wall, 3),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,

@@ -111,7 +111,14 @@ typedef struct are_scene_desc {
 	float bg_b[3];              /* gradient top (d.y=+1) */
 	int32_t triangle_test;      /* ARE_TRI_* */
 	int32_t bvh_leaf_size;      /* max primitives per BVH leaf; 0 = default (4) */
+	int32_t bvh_build;          /* ARE_BVH_*: where the tree is built (same answers either way) */
 } are_scene_desc;
+
+enum {
+	ARE_BVH_HOST_SAH = 0,  /* binned SAH on the host (best trees; seconds for millions of primitives) */
+	ARE_BVH_DEVICE = 1     /* linear BVH over Morton codes on the GPU (milliseconds); scenes of at most
+	                          48 primitives, which are scanned linearly, always use the host build */
+};
 
 typedef struct are_scene are_scene; /* opaque: device-resident SoA + BVH */
 
@@ -164,7 +171,8 @@ typedef struct are_render_stats {
 	int64_t kernel_launches[4]; /* launches per kernel kind */
 	int32_t error_word;         /* device error bits, 0 = clean */
 	int32_t reserved_;
-	double aux[4];              /* are_render_guided: training samples, Adam steps, guided vertices, last loss */
+	double aux[4];              /* are_render: [0] segments traced by the end-of-render tail kernel;
+	                               are_render_guided: training samples, Adam steps, guided vertices, last loss */
 } are_render_stats;
 
 /* ---- entry points ------------------------------------------------------- */

@@ -1,0 +1,69 @@
+"""The BVH built on the device (bvh_build = ARE_BVH_DEVICE): a different
+tree, the same answers.  Closest hits must equal the host-SAH scene's bit
+for bit (primitive id, t, u, v), and so must rendered images."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from common import are, hit_ids, random_rays
+
+pytestmark = pytest.mark.gpu
+
+
+def both(arrays, leaf=0):
+    h = are.Scene(dataclasses.replace(arrays, bvh_build=are.BVH_HOST_SAH, bvh_leaf_size=leaf))
+    d = are.Scene(dataclasses.replace(arrays, bvh_build=are.BVH_DEVICE, bvh_leaf_size=leaf))
+    return h, d
+
+
+def same_hits(a, b):
+    assert np.array_equal(hit_ids(a), hit_ids(b))
+    m = hit_ids(a) >= 0
+    assert np.array_equal(a[m][:, [0, 2, 3]].view(np.uint32), b[m][:, [0, 2, 3]].view(np.uint32))
+
+
+def scene_rays(arrays, n, seed):
+    lo = np.array([arrays_box(arrays)[0]]).min()
+    hi = np.array([arrays_box(arrays)[1]]).max()
+    return random_rays(n, seed, lo=lo, hi=hi, t_min=1e-4, t_max=np.inf, camera=(0.5 * (lo + hi),) * 3)
+
+
+def arrays_box(a):
+    pts = []
+    if len(a.spheres):
+        pts += [a.spheres[:, :3] - a.spheres[:, 3:4], a.spheres[:, :3] + a.spheres[:, 3:4]]
+    if len(a.triangles):
+        pts += [a.triangles[:, 0:3], a.triangles[:, 3:6], a.triangles[:, 6:9]]
+    if len(a.quads):
+        pts += [a.quads[:, 0:3], a.quads[:, 0:3] + a.quads[:, 3:6] + a.quads[:, 6:9]]
+    p = np.concatenate(pts)
+    return p.min(), p.max()
+
+
+@pytest.mark.parametrize("leaf", [1, 4, 8])
+def test_mesh_hits_equal_host_build(gpu_lib, leaf):
+    s, cam, par = are.build_config(are.CONFIG_MESH, mesh_frequency=60)
+    h, d = both(s, leaf)
+    assert d.info()["max_leaf"] <= leaf and d.info()["prims"] == s.n_prims
+    rays = scene_rays(s, 400_000, 3 + leaf)
+    same_hits(h.intersect(rays)[0], d.intersect(rays)[0])
+
+
+def test_sphere_field_hits_and_image_equal_host_build(gpu_lib):
+    s, cam, par = are.build_config(are.CONFIG_SPHERE_FIELD, seed=5, mesh_frequency=20000)
+    h, d = both(s)
+    rays = scene_rays(s, 300_000, 9)
+    same_hits(h.intersect(rays)[0], d.intersect(rays)[0])
+    p = dict(par, width=96, height=64, spp=8, seed=4)
+    ih, _, _ = h.render(cam, p, with_var=False)
+    idv, _, _ = d.render(cam, p, with_var=False)
+    assert np.array_equal(ih, idv)
+
+
+def test_small_scenes_fall_back_to_the_host_build(gpu_lib):
+    s, cam, par = are.build_config(are.CONFIG_CORNELL)
+    h, d = both(s)
+    assert h.info() == d.info()
+    rays = scene_rays(s, 50_000, 1)
+    same_hits(h.intersect(rays)[0], d.intersect(rays)[0])
