@@ -241,6 +241,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__r
 	const int tid = threadIdx.x, wg = tid >> 7, lt = tid & 127, warp = tid >> 5;
 	if (n_dev) n = min(n, (int)*n_dev);
 	const int tiles = (n + 127) / 128;
+	if (blockIdx.x * TC_WG >= tiles) return;  // no tile for this block: skip the weight copy and tensor memory
 	const bool out_vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;  // rows are 192 bytes: float4 stores when aligned
 	if (tid == 0) {
 		for (int b = 0; b < 1 + TC_WG; ++b) mbar_init(&bar[b], 1);

@@ -527,7 +527,9 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
 	const int g_tail = grid_for((const void *)k_tail, sc->n_sms);
-	const unsigned tail_max = (unsigned)std::max<int64_t>(8192, P / 16);  // queued paths below which the tail runs
+	// queued paths below which the tail kernel takes over (once every item is taken): its time is set
+	// by the longest remaining path, not by how many paths are left, so it can start early
+	const unsigned tail_max = (unsigned)std::max<int64_t>(8192, P / 4);
 	const DevScene S = sc->dev;
 
 	unsigned init[8] = { (unsigned)std::min<int64_t>(P, W.n_items), 0u, 0u, (unsigned)std::min<int64_t>(P, W.n_items),

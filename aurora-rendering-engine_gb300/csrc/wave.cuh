@@ -10,7 +10,7 @@
 
 namespace are_core {
 
-constexpr int GRAPH_ITERS = 16;  // iterations per graph launch (even)
+constexpr int GRAPH_ITERS = 8;  // iterations per graph launch (even)
 constexpr int BLOCK = 256;
 
 struct Wave {
