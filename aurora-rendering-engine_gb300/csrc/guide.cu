@@ -546,57 +546,100 @@ __global__ void __launch_bounds__(GT, 1) k_guide_fwdbwd(const __half *__restrict
 	if (lane == 0) atomicAdd(loss_sum, lacc);
 }
 
-// dW[o][i] += sum over a chunk of samples of delta[s][o] * h[s][i] on the tensor cores.
-__device__ __forceinline__ uint32_t pack2(const __half *p, size_t stride) {
+// dW[o][i] += sum over a chunk of samples of delta[s][o] * h[s][i] on the tensor
+// cores (mma.sync m16n8k16: M = outputs, N = inputs, K = samples).  The chunk
+// is staged in shared memory WG_SUB samples at a time with 16-byte loads (the
+// per-sample rows are contiguous), and each warp keeps the accumulators of its
+// output x input tiles in registers across the chunk, so the FP32 atomics
+// that merge blocks happen once per chunk.
+constexpr int WG_CHUNK = 256;  // samples per block
+constexpr int WG_SUB = 64;     // samples staged at a time
+constexpr int WG_PAD = 8;      // halves of padding per staged row (bank spread)
+constexpr size_t WG_SMEM = (size_t)WG_SUB * (GN_H + WG_PAD) * 2 + (size_t)WG_SUB * (GN_ENC + WG_PAD) * 2;
+
+__device__ __forceinline__ uint32_t pack2(const __half *p, int stride) {
 	__half2 v = __halves2half2(p[0], p[stride]);
 	return h2u(v);
 }
 
-template <int OUT_TILES, int IN_TILES>
-__device__ void wgrad_layer(const __half *__restrict__ D, int dstride, const __half *__restrict__ H, int hstride, int s0,
-	int s1, float *__restrict__ grad, int gstride, int out_limit, unsigned *overflow) {
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	const int ntiles = OUT_TILES * IN_TILES;
-	for (int tile = warp; tile < ntiles; tile += GT / 32) {
-		int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
-		float c[4] = { 0.f, 0.f, 0.f, 0.f };
-		for (int s = s0; s < s1; s += 16) {
-			uint32_t a[4];
-			const __half *dp = D + (size_t)(s + 2 * t) * dstride + ot * 16 + g;
-			a[0] = pack2(dp, dstride);
-			a[1] = pack2(dp + 8, dstride);
-			a[2] = pack2(dp + (size_t)8 * dstride, dstride);
-			a[3] = pack2(dp + (size_t)8 * dstride + 8, dstride);
-			const __half *hp = H + (size_t)(s + 2 * t) * hstride + it * 8 + g;
-			uint32_t b0 = pack2(hp, hstride), b1 = pack2(hp + (size_t)8 * hstride, hstride);
-			mma16816(c, a, b0, b1);
-		}
-		int o0 = ot * 16 + g, i0 = it * 8 + 2 * t;
-		bool bad = !(isfinite(c[0]) && isfinite(c[1]) && isfinite(c[2]) && isfinite(c[3]));
-		if (bad) atomicOr(overflow, 1u);
-		if (o0 < out_limit) atomicAdd(&grad[o0 * gstride + i0], c[0]), atomicAdd(&grad[o0 * gstride + i0 + 1], c[1]);
-		if (o0 + 8 < out_limit)
-			atomicAdd(&grad[(o0 + 8) * gstride + i0], c[2]), atomicAdd(&grad[(o0 + 8) * gstride + i0 + 1], c[3]);
+// rows [s, s + WG_SUB) of a [samples][width] FP16 matrix -> shared memory with row stride width + WG_PAD
+template <int WIDTH>
+__device__ __forceinline__ void stage_rows(const __half *__restrict__ src, int s, __half *dst) {
+	constexpr int V = WIDTH / 8;  // uint4 per row
+	for (int e = threadIdx.x; e < WG_SUB * V; e += blockDim.x) {
+		const int r = e / V, c = e - r * V;
+		*reinterpret_cast<uint4 *>(dst + r * (WIDTH + WG_PAD) + 8 * c) =
+			*reinterpret_cast<const uint4 *>(src + (size_t)(s + r) * WIDTH + 8 * c);
 	}
 }
 
-constexpr int WG_CHUNK = 512;
+template <int OUT_TILES, int IN_TILES, int DW, int HW>
+__device__ void wgrad_layer(const __half *__restrict__ D, const __half *__restrict__ H, int s0, int s1,
+	float *__restrict__ grad, int out_limit, unsigned *overflow, __half *sD, __half *sH) {
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	constexpr int NT = OUT_TILES * IN_TILES, PER = (NT + GT / 32 - 1) / (GT / 32);
+	constexpr int DS = DW + WG_PAD, HS = HW + WG_PAD;
+	float c[PER][4];
+#pragma unroll
+	for (int k = 0; k < PER; ++k) c[k][0] = c[k][1] = c[k][2] = c[k][3] = 0.f;
+	for (int s = s0; s < s1; s += WG_SUB) {
+		__syncthreads();
+		stage_rows<DW>(D, s, sD);
+		stage_rows<HW>(H, s, sH);
+		__syncthreads();
+#pragma unroll
+		for (int k = 0; k < PER; ++k) {
+			const int tile = warp + k * (GT / 32);
+			if (tile >= NT) break;
+			const int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
+#pragma unroll
+			for (int kk = 0; kk < WG_SUB; kk += 16) {
+				uint32_t a[4];
+				const __half *dp = sD + (kk + 2 * t) * DS + ot * 16 + g;
+				a[0] = pack2(dp, DS);
+				a[1] = pack2(dp + 8, DS);
+				a[2] = pack2(dp + 8 * DS, DS);
+				a[3] = pack2(dp + 8 * DS + 8, DS);
+				const __half *hp = sH + (kk + 2 * t) * HS + it * 8 + g;
+				mma16816(c[k], a, pack2(hp, HS), pack2(hp + 8 * HS, HS));
+			}
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < PER; ++k) {
+		const int tile = warp + k * (GT / 32);
+		if (tile >= NT) break;
+		const int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
+		const int o0 = ot * 16 + g, i0 = it * 8 + 2 * t;
+		if (!(isfinite(c[k][0]) && isfinite(c[k][1]) && isfinite(c[k][2]) && isfinite(c[k][3]))) atomicOr(overflow, 1u);
+		if (o0 < out_limit) atomicAdd(&grad[o0 * HW + i0], c[k][0]), atomicAdd(&grad[o0 * HW + i0 + 1], c[k][1]);
+		if (o0 + 8 < out_limit)
+			atomicAdd(&grad[(o0 + 8) * HW + i0], c[k][2]), atomicAdd(&grad[(o0 + 8) * HW + i0 + 1], c[k][3]);
+	}
+}
 
 __global__ void __launch_bounds__(GT) k_guide_wgrad(GuideTrainBufs B, int n, float *__restrict__ grad, unsigned *overflow) {
-	// samples are padded to a multiple of 16 with zero gradients
-	int s0 = blockIdx.x * WG_CHUNK, s1 = min(s0 + WG_CHUNK, n);
+	// samples are padded to a multiple of 16 with zero gradients; a partial last
+	// sub-chunk reads rows up to the next multiple of WG_SUB, which the training
+	// buffers hold (ensure_train rounds their capacity up)
+	extern __shared__ __align__(16) unsigned char wsm[];
+	__half *sD = reinterpret_cast<__half *>(wsm);
+	__half *sH = sD + WG_SUB * (GN_H + WG_PAD);
+	const int s0 = blockIdx.x * WG_CHUNK, s1 = min(s0 + WG_CHUNK, n);
 	if (s0 >= s1) return;
-	wgrad_layer<4, 32>(B.d[0], GN_H, B.h0, GN_ENC, s0, s1, grad + OFF_W1, GN_ENC, GN_H, overflow);
-	wgrad_layer<4, 8>(B.d[1], GN_H, B.h[0], GN_H, s0, s1, grad + OFF_W2, GN_H, GN_H, overflow);
-	wgrad_layer<4, 8>(B.d[2], GN_H, B.h[1], GN_H, s0, s1, grad + OFF_W3, GN_H, GN_H, overflow);
-	wgrad_layer<4, 8>(B.d[3], GN_H, B.h[2], GN_H, s0, s1, grad + OFF_W4, GN_H, GN_H, overflow);
-	wgrad_layer<3, 8>(B.d5, GN_OUT, B.h[3], GN_H, s0, s1, grad + OFF_W5, GN_H, 40, overflow);
+	wgrad_layer<4, 32, GN_H, GN_ENC>(B.d[0], B.h0, s0, s1, grad + OFF_W1, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[1], B.h[0], s0, s1, grad + OFF_W2, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[2], B.h[1], s0, s1, grad + OFF_W3, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[3], B.h[2], s0, s1, grad + OFF_W4, GN_H, overflow, sD, sH);
+	wgrad_layer<3, 8, GN_OUT, GN_H>(B.d5, B.h[3], s0, s1, grad + OFF_W5, 40, overflow, sD, sH);
 }
+
+constexpr int BG_CHUNK = 256;  // samples per block of k_guide_bgrad
 
 __global__ void k_guide_bgrad(GuideTrainBufs B, int n, float *__restrict__ grad) {
 	int col = threadIdx.x;  // 0..303
 	if (col >= 4 * GN_H + GN_OUT) return;
-	int s0 = blockIdx.x * 1024, s1 = min(s0 + 1024, n);
+	int s0 = blockIdx.x * BG_CHUNK, s1 = min(s0 + BG_CHUNK, n);
 	float acc = 0.f;
 	if (col < 4 * GN_H) {
 		int L = col / GN_H, o = col - L * GN_H;
@@ -718,7 +761,7 @@ are_status GuideNet::pack() {
 }
 
 are_status GuideNet::ensure_train(int n) {
-	int cap = (n + 15) & ~15;
+	int cap = (n + WG_SUB - 1) / WG_SUB * WG_SUB;  // k_guide_wgrad stages whole WG_SUB-row blocks
 	if (cap <= train_cap) return ARE_OK;
 	if (train_mem) cudaFree(train_mem);
 	train_mem = nullptr;
@@ -753,15 +796,16 @@ are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_
 are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaStream_t s) {
 	if (are_status st = ensure_train(n)) return st;
 	int np = (n + 15) & ~15;
+	const int nz = (n + WG_SUB - 1) / WG_SUB * WG_SUB;
 	cudaMemsetAsync(grad, 0, (GN_PARAMS + 64) * sizeof(float), s);
-	// rows n..np-1 of the training buffers are zero gradients
-	if (np > n) {
+	// rows n..nz-1 of the training buffers are zero (no gradient, no activation)
+	if (nz > n) {
 		for (int L = 0; L < 4; ++L) {
-			cudaMemsetAsync(bufs.d[L] + (size_t)n * GN_H, 0, (size_t)(np - n) * GN_H * 2, s);
-			cudaMemsetAsync(bufs.h[L] + (size_t)n * GN_H, 0, (size_t)(np - n) * GN_H * 2, s);
+			cudaMemsetAsync(bufs.d[L] + (size_t)n * GN_H, 0, (size_t)(nz - n) * GN_H * 2, s);
+			cudaMemsetAsync(bufs.h[L] + (size_t)n * GN_H, 0, (size_t)(nz - n) * GN_H * 2, s);
 		}
-		cudaMemsetAsync(bufs.d5 + (size_t)n * GN_OUT, 0, (size_t)(np - n) * GN_OUT * 2, s);
-		cudaMemsetAsync(bufs.h0 + (size_t)n * GN_ENC, 0, (size_t)(np - n) * GN_ENC * 2, s);
+		cudaMemsetAsync(bufs.d5 + (size_t)n * GN_OUT, 0, (size_t)(nz - n) * GN_OUT * 2, s);
+		cudaMemsetAsync(bufs.h0 + (size_t)n * GN_ENC, 0, (size_t)(nz - n) * GN_ENC * 2, s);
 	}
 	int tiles = np / 16;
 	int grid = std::max(1, std::min(n_sms, (tiles + 7) / 8));
@@ -774,8 +818,8 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 	}
 	k_guide_fwdbwd<<<grid, GT, guide_train_smem(), s>>>(img, bias, d_samples, n, wscale, wdev, weight_clip, loss_scale,
 		bufs, grad + GN_PARAMS);
-	k_guide_wgrad<<<(np + WG_CHUNK - 1) / WG_CHUNK, GT, 0, s>>>(bufs, np, grad, (unsigned *)(grad + GN_PARAMS + 1));
-	k_guide_bgrad<<<(np + 1023) / 1024, 320, 0, s>>>(bufs, np, grad);
+	k_guide_wgrad<<<(np + WG_CHUNK - 1) / WG_CHUNK, GT, WG_SMEM, s>>>(bufs, np, grad, (unsigned *)(grad + GN_PARAMS + 1));
+	k_guide_bgrad<<<(np + BG_CHUNK - 1) / BG_CHUNK, 320, 0, s>>>(bufs, np, grad);
 	return cuda_status(cudaGetLastError(), "guide gradient kernels");
 }
 

@@ -204,49 +204,43 @@ __device__ __forceinline__ void store_mixture(const Mixture &m, float *o) {
 		o[32 + 2 * l] = m.pi[l], o[33 + 2 * l] = m.norm[l];
 	}
 }
-__device__ __forceinline__ void load_mixture(const float *__restrict__ o, Mixture &m) {
-#pragma unroll
-	for (int l = 0; l < GN_LOBES; ++l) {
-		const float4 a = reinterpret_cast<const float4 *>(o)[l];
-		const float2 b = reinterpret_cast<const float2 *>(o + 32)[l];
-		m.mu[l] = f3{ a.x, a.y, a.z };
-		m.kappa[l] = a.w;
-		m.pi[l] = b.x;
-		m.norm[l] = b.y;
-	}
-}
 
-__device__ __forceinline__ float mixture_pdf(const Mixture &m, f3 w) {
+// Density and sampling of the packed mixture (store_mixture), read lobe by
+// lobe from memory so a shading thread does not hold the whole mixture in
+// registers.  Sampling picks a lobe by its weight, then draws the vMF sample
+// of W. Jakob's stable form, cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) /
+// kappa, azimuth 2 pi u2; the density is sum_l pi_l norm_l e^(kappa_l (mu_l.w - 1)).
+__device__ __forceinline__ float packed_pdf(const float *__restrict__ m, f3 w) {
 	float q = 0.f;
-#pragma unroll
+#pragma unroll 2
 	for (int l = 0; l < GN_LOBES; ++l) {
-		float c = m.mu[l].x * w.x + m.mu[l].y * w.y + m.mu[l].z * w.z;
-		q += m.pi[l] * m.norm[l] * __expf(m.kappa[l] * (c - 1.f));
+		const float4 a = reinterpret_cast<const float4 *>(m)[l];
+		const float2 b = reinterpret_cast<const float2 *>(m + 32)[l];
+		q += b.x * b.y * __expf(a.w * ((a.x * w.x + a.y * w.y + a.z * w.z) - 1.f));
 	}
 	return q;
 }
 
-// Draw a direction: lobe by u0, then the vMF sample of W. Jakob's stable form
-// cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) / kappa, azimuth 2 pi u2.
-__device__ __forceinline__ f3 mixture_sample(const Mixture &m, float u0, float u1, float u2) {
-	// the first lobe whose cumulative weight exceeds u0 (the last one if
-	// rounding leaves u0 above the total), selected without dynamic indexing
-	f3 z = m.mu[GN_LOBES - 1];
-	float k = m.kappa[GN_LOBES - 1], acc = 0.f;
-	bool found = false;
+__device__ __forceinline__ f3 packed_sample(const float *__restrict__ m, float u0, float u1, float u2) {
+	// the first lobe whose cumulative weight exceeds u0 (the last if rounding leaves u0 above the total)
+	int sel = GN_LOBES - 1;
+	float acc = 0.f;
 #pragma unroll
 	for (int l = 0; l < GN_LOBES - 1; ++l) {
-		acc += m.pi[l];
-		if (!found && u0 < acc) z = m.mu[l], k = m.kappa[l], found = true;
+		acc += m[32 + 2 * l];
+		if (sel == GN_LOBES - 1 && u0 < acc) sel = l;
 	}
+	const float4 a = reinterpret_cast<const float4 *>(m)[sel];
+	const float k = a.w;
 	float w = 1.f + logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k;
 	w = fminf(fmaxf(w, -1.f), 1.f);
 	float r = sqrtf(fmaxf(0.f, 1.f - w * w));
 	float s, c;
 	sincospif(2.f * u2, &s, &c);
-	f3 up = fabsf(z.z) < 0.999f ? f3{ 0.f, 0.f, 1.f } : f3{ 1.f, 0.f, 0.f };
-	f3 x = norm(cross(z, up));
-	f3 y = cross(z, x);
+	const f3 z = f3{ a.x, a.y, a.z };
+	const f3 up = fabsf(z.z) < 0.999f ? f3{ 0.f, 0.f, 1.f } : f3{ 1.f, 0.f, 0.f };
+	const f3 x = norm(cross(z, up));
+	const f3 y = cross(z, x);
 	return norm(add(add(scl(x, r * c), scl(y, r * s)), scl(z, w)));
 }
 

@@ -22,6 +22,7 @@
 
 #include "guide.cuh"
 #include "guide_host.h"
+#include "path.cuh"
 #include "scene.h"
 #include "wave.cuh"
 
@@ -45,53 +46,64 @@ struct GuidedState {
 	float rr_clip;
 };
 
-__device__ __forceinline__ unsigned lane_id_g() { return threadIdx.x & 31u; }
-__device__ __forceinline__ unsigned warp_append_g(unsigned *counter, bool pred) {
-	unsigned m = __ballot_sync(0xffffffffu, pred);
-	unsigned base = 0;
-	if (m) {
-		if (lane_id_g() == (unsigned)(__ffs(m) - 1)) base = atomicAdd(counter, (unsigned)__popc(m));
-		base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-	}
-	return base + (unsigned)__popc(m & ((1u << lane_id_g()) - 1u));
-}
-
-__global__ void __launch_bounds__(BLOCK) k_guide_select(DevScene S, Wave W, GuidedState G, int par) {
+// Closest hits of the queued rays (as k_intersect), then the network's input
+// list: every diffuse hit at depth < guide_depth gets its features written to
+// the compact list (its row in gidx), so inference runs on that list only.
+// The compact list's counter W.cnt[6] is zeroed before this kernel.
+__global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, GuidedState G, int par) {
+	__shared__ float4 snodes[2 * SMEM_NODES];
+	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
-	// the compact list's counter W.cnt[6] is zeroed before this kernel
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		W.cnt[par ^ 1] = 0;  // output queue of this iteration
+		atomicAdd(&W.stat[0], (unsigned long long)n);
+	}
+	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
+	const bool linear = S.n_prims <= LINEAR_MAX;
+	if (linear) {
+		stage_prims(S, snodes);
+		__syncthreads();
+	} else {
+		stage_nodes(S, snodes, n_snodes);
+	}
+	uint32_t err = 0;
+	const float inf = __int_as_float(0x7f800000);
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-		unsigned i = base + threadIdx.x;
+		const unsigned i = base + threadIdx.x;
 		bool sel = false;
 		float x[GN_IN];
 		if (i < n) {
-			float4 h = W.hit[i];
-			int leaf = __float_as_int(h.y);
-			int depth = __float_as_int(W.qb[par][i].w) & 0xff;
-			if (leaf >= 0 && depth < G.guide_depth) {
-				int mat = __ldg(S.prim_mat + leaf);
+			const float4 a = W.qa[par][i], b = W.qb[par][i];
+			const f3 o = ld3(a), d = ld3(b);
+			const Hit h = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, o, d, W.t_min, inf)
+								 : closest_hit(S, snodes, n_snodes, o, d, W.t_min, inf, err);
+			W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+			const int depth = __float_as_int(b.w) & 0xff;
+			if (h.leaf >= 0 && depth < G.guide_depth) {
+				const int mat = __ldg(S.prim_mat + h.leaf);
 				if (S.mats[mat].type == ARE_MAT_LAMBERTIAN) {
-					float4 a = W.qa[par][i], b = W.qb[par][i];
-					f3 o = ld3(a), d = ld3(b);
-					Surface sf = surface_at(S, leaf, o, d, h.x, h.z, h.w);
-					f3 nrm = dot(d, sf.ng) < 0.f ? sf.ng : scl(sf.ng, -1.f);
+					const Surface sf = surface_at(S, h.leaf, o, d, h.t, h.u, h.v);
+					const f3 nrm = dot(d, sf.ng) < 0.f ? sf.ng : scl(sf.ng, -1.f);
 					guide_features(G.box, sf.p, nrm, scl(d, -1.f), x);
 					sel = true;
 				}
 			}
 		}
-		unsigned pos = warp_append_g(&W.cnt[6], sel);
-		unsigned m = __ballot_sync(0xffffffffu, sel);
-		if ((threadIdx.x & 31) == 0 && m) atomicAdd(&W.stat[3], (unsigned long long)__popc(m));
+		const unsigned pos = warp_append(&W.cnt[6], sel);
+		const unsigned m = __ballot_sync(0xffffffffu, sel);
+		if (lane_id() == 0 && m) atomicAdd(&W.stat[3], (unsigned long long)__popc(m));
 		if (i < n) G.gidx[i] = sel ? (int)pos : -1;
 		if (sel)
 			for (int k = 0; k < GN_IN; ++k) G.gfeat[(size_t)pos * GN_IN + k] = x[k];
 	}
+	if (err) atomicOr(&W.cnt[4], err);
 }
 
 __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, GuidedState G, int par) {
 	const unsigned n = W.cnt[par];
 	const int out = par ^ 1;
 	uint32_t err = 0;
+	unsigned long long done = 0;
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		unsigned i = base + threadIdx.x;
 		bool valid = i < n;
@@ -134,13 +146,12 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 				int gi = G.gidx[i];
 				if (gi >= 0) {
 					// guided diffuse vertex: one-sample MIS of the vMF mixture and cosine sampling
-					Mixture M;
-					load_mixture(G.gout + (size_t)gi * GN_OUT, M);
+					const float *M = G.gout + (size_t)gi * GN_OUT;
 					f3 nrm = dot(d, sf.ng) < 0.f ? sf.ng : scl(sf.ng, -1.f);
 					uint32_t cb = ctr_bounce(depth);
 					f3 w;
 					if (uniform(key, cb + 4) < G.mix) {
-						w = mixture_sample(M, uniform(key, cb + 7), uniform(key, cb + 5), uniform(key, cb + 6));
+						w = packed_sample(M, uniform(key, cb + 7), uniform(key, cb + 5), uniform(key, cb + 6));
 					} else {
 						float r1 = uniform(key, cb), r2 = uniform(key, cb + 1);
 						float s, c;
@@ -151,7 +162,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 					float cosw = dot(w, nrm);
 					if (cosw > 0.f) {
 						const float inv_pi = 0.31830988618379067154f;
-						float pdf = G.mix * mixture_pdf(M, w) + (1.f - G.mix) * cosw * inv_pi;
+						float pdf = G.mix * packed_pdf(M, w) + (1.f - G.mix) * cosw * inv_pi;
 						const DevMaterial &m = S.mats[sf.mat];
 						f3 alb = tex_eval(S, m.texture, sf.u, sf.v, sf.p);
 						f3 L_before = L;
@@ -192,71 +203,63 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 			}
 			term = !cont;
 		}
-		unsigned pos = warp_append_g(&W.cnt[out], cont);
-		if (cont) {
-			if (pos < (unsigned)W.P) {
+		// a finished path: its recorded guided vertices become training samples
+		// (incident radiance L_in = (L_final - L_before) / beta_after along the
+		// sampled direction, weight lum(L_in) cos / pdf) ...
+		const int slot = __float_as_int(ra.w);
+		// vertices recorded by any finished path of the warp (warp-uniform)
+		const unsigned wmask = __reduce_or_sync(0xffffffffu, term ? vmask : 0u);
+		for (int v = 0; v < GV; ++v) {
+			if (!((wmask >> v) & 1u)) continue;
+			bool emit = false;
+			float4 o0, o1, o2, o3;
+			if (term && ((vmask >> v) & 1u)) {
+				const float4 *r = G.vrec + ((size_t)slot * GV + v) * 6;
+				const float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4], r5 = r[5];
+				const float li[3] = { r4.x > 0.f ? (L.x - r5.x) / r4.x : 0.f, r4.y > 0.f ? (L.y - r5.y) / r4.y : 0.f,
+					r4.z > 0.f ? (L.z - r5.z) / r4.z : 0.f };
+				const float lum = 0.2126f * li[0] + 0.7152f * li[1] + 0.0722f * li[2];
+				const float wt = lum * r3.y / r3.x;
+				if (wt > 0.f && isfinite(wt)) {
+					o0 = r0, o1 = r1, o2 = r2, o3 = make_float4(wt, 0.f, 0.f, 0.f);
+					emit = true;
+				}
+			}
+			const unsigned tpos = warp_append(G.tcount, emit);
+			const unsigned m = __ballot_sync(0xffffffffu, emit);
+			if (lane_id() == 0 && m) atomicAdd(&W.stat[2], (unsigned long long)__popc(m));
+			if (emit && tpos < G.tcap) {
+				float4 *o = reinterpret_cast<float4 *>(G.tbuf + (size_t)tpos * 16);
+				o[0] = o0, o[1] = o1, o[2] = o2, o[3] = o3;
+			}
+		}
+		// ... then the accumulate step and the slot's next camera path (as the plain shading kernel)
+		bool spawn = false;
+		PathState C;
+		if (term) {
+			++done;
+			int64_t item = (int64_t)(unsigned)__float_as_int(rc.w);
+			int j = __float_as_int(rb.w) >> 8;
+			spawn = finish_path(W, slot, L, item, j, err, &W.cnt[3]);
+			if (spawn) camera_path(W, slot, item, j, C);
+		}
+		const unsigned pos = warp_append(&W.cnt[out], cont || spawn);
+		if (cont || spawn) {
+			if (pos >= (unsigned)W.P) {
+				err |= ERR_QUEUE_OVERFLOW;
+			} else if (cont) {
 				W.qa[out][pos] = make_float4(p.x, p.y, p.z, ra.w);
 				W.qb[out][pos] = make_float4(nd.x, nd.y, nd.z, __int_as_float(__float_as_int(rb.w) + 1));
 				W.qc[out][pos] = make_float4(beta.x, beta.y, beta.z, rc.w);
 				W.qd[out][pos] = make_float4(L.x, L.y, L.z, __uint_as_float((__float_as_uint(rrs) & ~0xfu) | vmask));
 			} else {
-				err |= ERR_QUEUE_OVERFLOW;
-			}
-		}
-		unsigned tp = warp_append_g(&W.cnt[2], term);
-		if (term) {
-			if (tp < (unsigned)W.P) {
-				W.ta[tp] = make_float4(L.x, L.y, L.z, ra.w);
-				W.tb[tp] = make_float4(rc.w, __int_as_float(__float_as_int(rb.w) >> 8), __uint_as_float(vmask), 0.f);
-			} else {
-				err |= ERR_QUEUE_OVERFLOW;
+				store_path(W, out, pos, C);  // qd.w = 0: no recorded vertex, roulette scale 1
 			}
 		}
 	}
+	for (int o = 16; o > 0; o >>= 1) done += __shfl_down_sync(0xffffffffu, done, o);
+	if (lane_id() == 0 && done) atomicAdd(&W.stat[1], done);
 	if (err) atomicOr(&W.cnt[4], err);
-}
-
-// Finished paths: their recorded guided vertices become training samples,
-// then the plain generate step accumulates and starts the next camera path.
-__global__ void __launch_bounds__(BLOCK) k_emit_training(Wave W, GuidedState G) {
-	const unsigned n = W.cnt[2];
-	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-		unsigned i = base + threadIdx.x;
-		for (int v = 0; v < GV; ++v) {
-			bool emit = false;
-			float rec[13];
-			if (i < n && ((__float_as_uint(W.tb[i].z) >> v) & 1u)) {
-				float4 a = W.ta[i];
-				int slot = __float_as_int(a.w);
-				const float4 *r = G.vrec + ((size_t)slot * GV + v) * 6;
-				{
-					float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3], r4 = r[4], r5 = r[5];
-					// incident radiance estimate along the sampled direction
-					float li[3] = { r4.x > 0.f ? (a.x - r5.x) / r4.x : 0.f, r4.y > 0.f ? (a.y - r5.y) / r4.y : 0.f,
-						r4.z > 0.f ? (a.z - r5.z) / r4.z : 0.f };
-					float lum = 0.2126f * li[0] + 0.7152f * li[1] + 0.0722f * li[2];
-					float wt = lum * r3.y / r3.x;
-					if (wt > 0.f && isfinite(wt)) {
-						rec[0] = r0.x, rec[1] = r0.y, rec[2] = r0.z, rec[3] = r0.w;
-						rec[4] = r1.x, rec[5] = r1.y, rec[6] = r1.z, rec[7] = r1.w;
-						rec[8] = r2.x, rec[9] = r2.y, rec[10] = r2.z, rec[11] = r2.w;
-						rec[12] = wt;
-						emit = true;
-					}
-				}
-			}
-			unsigned pos = warp_append_g(G.tcount, emit);
-			unsigned m = __ballot_sync(0xffffffffu, emit);
-			if (lane_id_g() == 0 && m) atomicAdd(&W.stat[2], (unsigned long long)__popc(m));
-			if (emit && pos < G.tcap) {
-				float4 *o = reinterpret_cast<float4 *>(G.tbuf + (size_t)pos * 16);
-				o[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
-				o[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
-				o[2] = make_float4(rec[8], rec[9], rec[10], rec[11]);
-				o[3] = make_float4(rec[12], 0.f, 0.f, 0.f);
-			}
-		}
-	}
 }
 
 namespace {
@@ -325,7 +328,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	size_t need = 0;
 	char *z = nullptr;
 	for (int q = 0; q < 2; ++q) carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
-	carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
+	carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);  // hit, accumulators
 	carve<unsigned>(z, 64), carve<unsigned long long>(z, 8);
 	carve<int32_t>(z, P), carve<float>(z, (size_t)P * GN_IN), carve<float>(z, (size_t)P * GN_OUT);
 	carve<float4>(z, (size_t)P * GV * 6), carve<float>(z, (size_t)tcap * 16);
@@ -339,7 +342,6 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		W.qa[q] = carve<float4>(z, P), W.qb[q] = carve<float4>(z, P), W.qc[q] = carve<float4>(z, P),
 		W.qd[q] = carve<float4>(z, P);
 	W.hit = carve<float4>(z, P);
-	W.ta = carve<float4>(z, P), W.tb = carve<float4>(z, P);
 	W.acc_s = carve<float4>(z, P), W.acc_c = carve<float4>(z, P), W.acc_q = carve<float4>(z, P);
 	W.cnt = carve<unsigned>(z, 64);
 	W.stat = carve<unsigned long long>(z, 8);
@@ -374,24 +376,18 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_init");
 	}
-	const int g_int = grid_of((const void *)k_intersect, sc->n_sms);
-	const int g_sel = grid_of((const void *)k_guide_select, sc->n_sms);
+	const int g_int = grid_of((const void *)k_intersect_select, sc->n_sms);
 	const int g_sh = grid_of((const void *)k_shade_guided, sc->n_sms);
-	const int g_gen = grid_of((const void *)k_generate, sc->n_sms);
-	const int g_emit = grid_of((const void *)k_emit_training, sc->n_sms);
 	const DevScene S = sc->dev;
 	// the network runs on the compact list, its length read on the device
 	if (!st) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
 	if (!st) {
 		for (int it = 0; it < GUIDED_ITERS; ++it) {
 			int par = it & 1;
-			k_intersect<<<g_int, BLOCK, 0, s>>>(S, W, par);
 			cudaMemsetAsync(W.cnt + 6, 0, 4, s);
-			k_guide_select<<<g_sel, BLOCK, 0, s>>>(S, W, G, par);
+			k_intersect_select<<<g_int, BLOCK, 0, s>>>(S, W, G, par);
 			net->infer(G.gfeat, P, G.gout, s, W.cnt + 6, W.cnt + 4, true);
 			k_shade_guided<<<g_sh, BLOCK, 0, s>>>(S, W, G, par);
-			k_emit_training<<<g_emit, BLOCK, 0, s>>>(W, G);
-			k_generate<<<g_gen, BLOCK, 0, s>>>(W, par);
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "capture end");
 	}
@@ -410,8 +406,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		if (st) break;
 		iterations += GUIDED_ITERS;
 		launches[ARE_KERNEL_INTERSECT] += GUIDED_ITERS;
-		launches[ARE_KERNEL_SHADE] += 3 * GUIDED_ITERS;
-		launches[ARE_KERNEL_GENERATE] += 2 * GUIDED_ITERS;
+		launches[ARE_KERNEL_SHADE] += 2 * GUIDED_ITERS;  // inference, shade (+ training samples, accumulate, generate)
 		const unsigned have = std::min(hc[7], tcap);
 		if (pending_loss) {
 			// the loss of the step enqueued after the previous launch is complete now

@@ -36,7 +36,7 @@ namespace are_core {
 
 namespace {
 
-constexpr size_t NA_SLOT_BYTES = WAVE_SLOT_BYTES;  // queues, hit, finished record, accumulators
+constexpr size_t NA_SLOT_BYTES = WAVE_SLOT_BYTES;  // queues, hit, accumulators
 constexpr size_t NA_ITEM_BYTES = 2 * sizeof(float4);                  // per-pixel sum and sum of squares
 constexpr size_t NA_SCRATCH = (size_t)ARE_NOALLOC_MAX_PATHS * NA_SLOT_BYTES + (size_t)ARE_NOALLOC_MAX_PIXELS * NA_ITEM_BYTES +
 	64 * sizeof(unsigned) + 8 * sizeof(unsigned long long) + 18 * 256;  // 18 arrays, each padded to 256 bytes
@@ -126,7 +126,6 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 		W.qa[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.qb[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS),
 		W.qc[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.qd[q] = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.hit = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
-	W.ta = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.tb = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.acc_s = take<float4>(z, ARE_NOALLOC_MAX_PATHS), W.acc_c = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.acc_q = take<float4>(z, ARE_NOALLOC_MAX_PATHS);
 	W.item_s = take<float4>(z, ARE_NOALLOC_MAX_PIXELS);

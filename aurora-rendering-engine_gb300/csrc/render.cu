@@ -2,22 +2,23 @@
 //
 // Replaces rt.cpp render() / trace() / intersect() (experiments/rt.cpp:209-374).
 // The reference walks pixels one by one and recurses per path on one host
-// thread.  Here a pool of P paths lives in HBM as SoA records and every
-// wavefront iteration runs three kernels over compacted queues:
+// thread.  Here a pool of P paths lives in HBM as 64-byte SoA queue records
+// (the path state travels with its ray) and every wavefront iteration runs two
+// kernels over compacted queues:
 //
-//   intersect : closest hit of every queued ray (BVH, top levels in smem)
-//   shade     : emission + material scatter + Russian roulette; surviving
-//               paths append their next ray to the output queue, finished
-//               paths append their slot to the terminated list (warp-ballot
-//               compaction, one atomic per warp)
-//   generate  : finished paths add their radiance to the slot's Kahan sum,
-//               take their next sample (or next work item) and append a new
-//               camera ray to the output queue
+//   intersect : closest hit of every queued ray (BVH with its top levels in
+//               shared memory, or a linear scan of tiny scenes)
+//   shade     : emission + material scatter + Russian roulette; a surviving
+//               path appends its next ray to the output queue; a finished
+//               path adds its radiance to its slot's Kahan sum, takes its
+//               next sample (or next work item) and appends that camera ray
+//               instead (warp-ballot compaction, one atomic per warp)
 //
 // Work items are (pixel, chunk of samples); each item's samples run in one
 // slot in order, so the per-item Kahan sums - and the image - do not depend
 // on scheduling.  `resolve` adds the items of each pixel in chunk order.
-// Iterations are captured K at a time in a CUDA graph.
+// Iterations are captured K at a time in a CUDA graph; when every item is
+// taken and few paths remain, `tail` finishes them in one launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,29 +29,11 @@
 
 #include "scene.h"
 #include "shade.cuh"
+#include "path.cuh"
 #include "traverse.cuh"
 #include "wave.cuh"
 
 namespace are_core {
-
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
-
-// Warp-aggregated append: every lane of the (converged) warp calls this.
-__device__ __forceinline__ unsigned warp_append(unsigned *counter, bool pred) {
-	unsigned m = __ballot_sync(0xffffffffu, pred);
-	unsigned base = 0;
-	if (m) {
-		if (lane_id() == (unsigned)(__ffs(m) - 1)) base = atomicAdd(counter, (unsigned)__popc(m));
-		base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-	}
-	return base + (unsigned)__popc(m & ((1u << lane_id()) - 1u));
-}
-
-__device__ __forceinline__ void stage_nodes(const DevScene &S, float4 *snodes, int &n_snodes) {
-	n_snodes = min(S.n_nodes, SMEM_NODES);
-	for (int i = threadIdx.x; i < 2 * n_snodes; i += blockDim.x) snodes[i] = __ldg(S.nodes + i);
-	__syncthreads();
-}
 
 // ---------------------------------------------------------------------------
 // batched closest hit (are_intersect)
@@ -83,26 +66,6 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 
 // ---------------------------------------------------------------------------
 // wavefront kernels
-
-__device__ __forceinline__ void item_coords(const Wave &W, int64_t item, int j, int &pixel, int &sample) {
-	const uint32_t it = (uint32_t)item, np = (uint32_t)W.npix;  // n_items < 2^32 (checked on the host)
-	const uint32_t chunk = it / np;
-	pixel = (int)(it - chunk * np);
-	sample = (int)chunk * W.chunk + j;
-}
-
-// queue record of a fresh camera path for (item, j) in `slot`
-__device__ __forceinline__ void put_camera_ray(const Wave &W, int q, unsigned pos, int slot, int64_t item, int j) {
-	int pixel, sample;
-	item_coords(W, item, j, pixel, sample);
-	uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
-	f3 o, d;
-	camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, o, d);
-	W.qa[q][pos] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
-	W.qb[q][pos] = make_float4(d.x, d.y, d.z, __int_as_float(j << 8));
-	W.qc[q][pos] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)item));
-	W.qd[q][pos] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
 
 __global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
 	// slot s takes work item s; its first camera ray goes to queue 0 position s
@@ -142,74 +105,6 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 		W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}
 	if (err) atomicOr(&W.cnt[4], err);
-}
-
-// Kahan accumulation of a finished path's radiance L into its slot, in sample
-// order; when the slot's work item is complete its sums are published and the
-// slot takes the next item from *next_item.  Returns whether the slot has a
-// next sample (item, j).
-__device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64_t &item, int &j, uint32_t &err,
-	unsigned *next_item) {
-	if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
-		err |= ERR_NONFINITE;
-		L = f3{ 0.f, 0.f, 0.f };
-	}
-	float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
-	float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
-	float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
-	cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
-	sm = make_float4(ts[0], ts[1], ts[2], 0.f);
-	q = make_float4(q.x + L.x * L.x, q.y + L.y * L.y, q.z + L.z * L.z, 0.f);
-	++j;
-	int chunk_len = min(W.chunk, W.spp - (int)((uint32_t)item / (uint32_t)W.npix) * W.chunk);
-	if (j >= chunk_len) {
-		// item complete: publish its sums, take the next item
-		W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
-		W.item_q[item] = q;
-		sm = cm = q = make_float4(0.f, 0.f, 0.f, 0.f);
-		item = (int64_t)atomicAdd(next_item, 1u);
-		j = 0;
-	}
-	W.acc_s[slot] = sm;
-	W.acc_c[slot] = cm;
-	W.acc_q[slot] = q;
-	return item < W.n_items;
-}
-
-// A path between bounces: its ray and the state that travels with it.
-struct PathState {
-	f3 o, d, beta, L;
-	int slot, depth, j;
-	int64_t item;
-};
-
-__device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i) {
-	const float4 ra = W.qa[q][i], rb = W.qb[q][i], rc = W.qc[q][i], rd = W.qd[q][i];
-	PathState P;
-	P.o = ld3(ra), P.d = ld3(rb), P.beta = ld3(rc), P.L = ld3(rd);
-	P.slot = __float_as_int(ra.w);
-	const int meta = __float_as_int(rb.w);
-	P.depth = meta & 0xff, P.j = meta >> 8;
-	P.item = (int64_t)(unsigned)__float_as_int(rc.w);
-	return P;
-}
-
-__device__ __forceinline__ void store_path(const Wave &W, int q, unsigned pos, const PathState &P) {
-	W.qa[q][pos] = make_float4(P.o.x, P.o.y, P.o.z, __int_as_float(P.slot));
-	W.qb[q][pos] = make_float4(P.d.x, P.d.y, P.d.z, __int_as_float(P.depth | (P.j << 8)));
-	W.qc[q][pos] = make_float4(P.beta.x, P.beta.y, P.beta.z, __int_as_float((int)P.item));
-	W.qd[q][pos] = make_float4(P.L.x, P.L.y, P.L.z, 0.f);
-}
-
-// The first ray of sample j of work item `item`, as put_camera_ray writes it.
-__device__ __forceinline__ void camera_path(const Wave &W, int slot, int64_t item, int j, PathState &P) {
-	int pixel, sample;
-	item_coords(W, item, j, pixel, sample);
-	uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
-	camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, P.o, P.d);
-	P.beta = f3{ 1.f, 1.f, 1.f };
-	P.L = f3{ 0.f, 0.f, 0.f };
-	P.slot = slot, P.depth = 0, P.j = j, P.item = item;
 }
 
 // One bounce of path P at hit h (t, leaf bits, u, v): scatter and, when the
@@ -315,41 +210,6 @@ __global__ void __launch_bounds__(BLOCK) k_tail(DevScene S, Wave W, int par) {
 		if (done) atomicAdd(&W.stat[1], done);
 		if (segments) atomicAdd(&W.stat[0], segments), atomicAdd(&W.stat[2], segments);
 	}
-	if (err) atomicOr(&W.cnt[4], err);
-}
-
-// The accumulate and generate steps on their own, for estimators whose
-// shading pass lists finished paths (ta/tb) for further use.
-__global__ void __launch_bounds__(BLOCK) k_generate(Wave W, int par) {
-	const unsigned n = W.cnt[2];
-	const int out = par ^ 1;
-	uint32_t err = 0;
-	unsigned long long done = 0;
-	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-		unsigned i = base + threadIdx.x;
-		bool valid = i < n;
-		bool emit = false;
-		int slot = 0, j = 0;
-		int64_t item = 0;
-		if (valid) {
-			float4 a = W.ta[i], b = W.tb[i];
-			slot = __float_as_int(a.w);
-			item = (int64_t)(unsigned)__float_as_int(b.x);
-			j = __float_as_int(b.y);
-			++done;
-			emit = finish_path(W, slot, ld3(a), item, j, err, &W.cnt[3]);
-		}
-		unsigned pos = warp_append(&W.cnt[out], emit);
-		if (emit) {
-			if (pos < (unsigned)W.P)
-				put_camera_ray(W, out, pos, slot, item, j);
-			else
-				err |= ERR_QUEUE_OVERFLOW;
-		}
-	}
-	// one atomic per warp: every lane of the block reaches this point
-	for (int o = 16; o > 0; o >>= 1) done += __shfl_down_sync(0xffffffffu, done, o);
-	if (lane_id() == 0 && done) atomicAdd(&W.stat[1], done);
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
@@ -473,7 +333,6 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		for (int q = 0; q < 2; ++q)
 			carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
 		carve<float4>(z, P);                      // hit
-		carve<float4>(z, P), carve<float4>(z, P);  // finished records
 		carve<float4>(z, P), carve<float4>(z, P), carve<float4>(z, P);
 		carve<unsigned>(z, 64);
 		carve<unsigned long long>(z, 8);
@@ -501,7 +360,6 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			W.qa[q] = carve<float4>(z, P), W.qb[q] = carve<float4>(z, P), W.qc[q] = carve<float4>(z, P),
 			W.qd[q] = carve<float4>(z, P);
 		W.hit = carve<float4>(z, P);
-		W.ta = carve<float4>(z, P), W.tb = carve<float4>(z, P);
 		W.acc_s = carve<float4>(z, P), W.acc_c = carve<float4>(z, P), W.acc_q = carve<float4>(z, P);
 		W.cnt = carve<unsigned>(z, 64);
 		W.stat = carve<unsigned long long>(z, 8);

@@ -223,6 +223,14 @@ struct Hit {
 
 __device__ __forceinline__ float4 ldg4(const float4 *p) { return __ldg(p); }
 
+// Stages the first SMEM_NODES BVH nodes (the breadth-first top levels) into
+// shared memory.
+__device__ __forceinline__ void stage_nodes(const DevScene &S, float4 *snodes, int &n_snodes) {
+	n_snodes = min(S.n_nodes, SMEM_NODES);
+	for (int i = threadIdx.x; i < 2 * n_snodes; i += blockDim.x) snodes[i] = __ldg(S.nodes + i);
+	__syncthreads();
+}
+
 // Stages the primitives of a scene with at most LINEAR_MAX of them into
 // shared memory: per primitive [0..2] the leaf-order record (global id in
 // [1].w), [3] the quad normal u x v and its squared length; then, from

@@ -21,11 +21,10 @@ struct Wave {
 	// its records in queue order; only the per-slot accumulators are gathered.
 	float4 *qa[2], *qb[2], *qc[2], *qd[2];
 	float4 *hit;      // (t, leaf bits, u, v) per queue position
-	float4 *ta, *tb;  // finished paths: (radiance, slot bits), (item bits, j bits, 0, 0)
 	float4 *acc_s;    // Kahan sum (xyz) per slot
 	float4 *acc_c;    // Kahan compensation per slot
 	float4 *acc_q;    // sum of squares per slot
-	unsigned *cnt;    // [0],[1] queue sizes, [2] finished, [3] next work item, [4] error word
+	unsigned *cnt;    // [0],[1] queue sizes, [3] next work item, [4] error word, [6], [7] guided counters
 	unsigned long long *stat;  // [0] segments, [1] samples
 	float4 *item_s;   // per work item: sum (xyz)
 	float4 *item_q;   // per work item: sum of squares
@@ -38,8 +37,8 @@ struct Wave {
 	CameraFrame cam;
 };
 
-// bytes of wavefront state per path slot (queues x 2, hit, finished record, accumulators)
-constexpr size_t WAVE_SLOT_BYTES = 2 * 4 * sizeof(float4) + sizeof(float4) + 2 * sizeof(float4) + 3 * sizeof(float4);
+// bytes of wavefront state per path slot (queues x 2, hit, accumulators)
+constexpr size_t WAVE_SLOT_BYTES = 2 * 4 * sizeof(float4) + sizeof(float4) + 3 * sizeof(float4);
 
 // rt.cpp:339-343 camera basis (host)
 void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);
@@ -47,7 +46,7 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);
 __global__ void k_init(Wave W, int n_first);
 __global__ void k_intersect(DevScene S, Wave W, int par);
 __global__ void k_shade(DevScene S, Wave W, int par);
-__global__ void k_generate(Wave W, int par);
+__global__ void k_tail(DevScene S, Wave W, int par);
 __global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ var, int clamp);
 
 }  // namespace are_core

@@ -49,6 +49,7 @@ WORKLOADS = {
     "mesh": (2, "displaced_icosphere_2M_tris_1920x1080_256spp_depth16"),
     "batch": (6, "uneven_batch_64_sphere_fields_50_to_200k_one_launch"),
     "guided": (4, "cornell_occluded_600x600_1024spp_depth16_guided"),
+    "legacy": (5, "rt_cpp_scene_512x512_reference_estimator"),
 }
 WORKLOAD = WORKLOADS["cornell"][1]
 # algorithmic bytes of the wavefront's compulsory SoA traffic
@@ -365,6 +366,86 @@ def run_guided(args, rank, world) -> None:
     sc.close()
 
 
+def run_legacy(args, rank, world) -> None:
+    """--workload legacy: the reference's own scene and estimator (rt.cpp's
+    34 triangles; per pixel 32 ambient-occlusion rays, the depth-0 mirror and
+    32 diffuse paths of up to 3 bounces, experiments/rt.cpp:221-374) at its
+    own 512x512, one trace per pixel; a "sample" is one pixel's trace."""
+    import torch
+
+    import are_gb300 as are
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    scene_arrays, cam, par = are.build_config(are.CONFIG_LEGACY_RT)
+    W, H = par["width"], par["height"]
+    sc = are.Scene(scene_arrays)
+    rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    reps = 64  # frames per step: one frame is about a millisecond
+    for i in range(args.warmup):
+        sc.render_device(cam, dict(par, seed=100 + i), rgb.data_ptr())
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    stats = []
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            for r in range(reps):
+                stats.append(sc.render_device(cam, dict(par, seed=1 + i * reps + r), rgb.data_ptr()))
+    torch.cuda.synchronize()
+    barrier(world)
+    dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
+    px = W * H * len(stats)
+    value = world * px / (dev_ms / 1e3) / 1e6
+    # end to end: scene from the host descriptor, host image, scene freed
+    e2e_t = []
+    for i in range(3):
+        t0 = time.perf_counter()
+        s2 = are.Scene(scene_arrays)
+        s2.render(cam, dict(par, seed=500 + i), with_var=False)
+        s2.close()
+        e2e_t.append(time.perf_counter() - t0)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle.orc import Oracle, render_legacy
+
+        orc = Oracle()
+        ctx = orc.prepare(scene_arrays, accel=0)
+        threads = os.cpu_count() or 1
+        t = time.perf_counter()
+        render_legacy(orc, ctx, cam, par, rng_mode=0, nthreads=threads)
+        dt = time.perf_counter() - t
+        cpu = {"value": round(W * H / dt / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the whole {W}x{H} frame ({dt:.2f} s): the oracle's restatement of rt.cpp's estimator "
+                         f"(rt.cpp itself is not on this host)"}
+    ms_frame = dev_ms / len(stats)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["legacy"][1], "width": W, "height": H, "frames_per_step": reps,
+                       "queries_per_pixel": 66, "parallelism": f"replicas{world}",
+                       "l2": "flushed (256 MB write) between steps; scene in shared memory"},
+            "ms_per_frame": round(ms_frame, 4),
+            "e2e": {"value": round(W * H / statistics.median(e2e_t) / 1e6 * world, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(x.nbytes for x in scene_arrays.__dict__.values() if hasattr(x, "nbytes"))),
+                    "d2h_bytes_per_step": W * H * 12},
+            "roofline": {"kernel": "legacy", "bound": "hbm", "achieved": round(W * H * 12 / (ms_frame / 1e3) / 1e9, 2),
+                         "peak": measured_peaks()["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(W * H * 12 / (ms_frame / 1e3) / 1e9 / measured_peaks()["hbm_gbs"], 6),
+                         "traffic": None, "note": "66 closest-hit queries per pixel over 34 triangles in shared "
+                                                  "memory: issue-bound, the 12 output bytes are all it moves"},
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": sum(sum(s["kernel_launches"].values()) for s in stats),
+        }
+        print(json.dumps(line), flush=True)
+    sc.close()
+
+
 def run_reference(args, rank, world) -> None:
     """--impl reference: the CPU implementation of the path on the host cores."""
     if rank != 0:
@@ -425,8 +506,8 @@ def main() -> None:
             pg.destroy_process_group()
         return
 
-    if args.workload in ("batch", "guided"):
-        (run_batch if args.workload == "batch" else run_guided)(args, rank, world)
+    if args.workload in ("batch", "guided", "legacy"):
+        {"batch": run_batch, "guided": run_guided, "legacy": run_legacy}[args.workload](args, rank, world)
         if pg:
             pg.destroy_process_group()
         return
