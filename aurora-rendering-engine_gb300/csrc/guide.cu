@@ -472,7 +472,7 @@ __device__ __forceinline__ void store_a64(const uint32_t (*a)[4], __half *base, 
 __global__ void __launch_bounds__(GT, 1) k_guide_fwdbwd(const __half *__restrict__ img, const float *__restrict__ bias,
 	const float *__restrict__ samples, int n, float wscale, const float *__restrict__ wscale_dev, float wclip, float lscale,
 	GuideTrainBufs B, float *__restrict__ loss_sum) {
-	if (wscale_dev) wscale = *wscale_dev;
+	if (wscale_dev) wscale = *wscale_dev > 0.f ? (float)n / *wscale_dev : 0.f;  // device sum of the weights
 	extern __shared__ __align__(16) unsigned char smem[];
 	__half *s_img = reinterpret_cast<__half *>(smem);
 	float *s_bias = reinterpret_cast<float *>(smem + IMG_ALL * sizeof(__half));
@@ -669,17 +669,20 @@ __global__ void k_guide_adam(float *__restrict__ P, float *__restrict__ m, float
 }
 
 // n / (sum of the batch's weights) -> *out
-__global__ void k_weight_scale(const float *__restrict__ samples, int n, float *__restrict__ out) {
+// sum of the batch's sample weights into *out (zeroed before), many blocks;
+// the forward/backward kernel turns it into the mean-weight scale n / sum
+__global__ void k_weight_sum(const float *__restrict__ samples, int n, float *__restrict__ out) {
 	__shared__ float red[256];
 	float acc = 0.f;
-	for (int i = threadIdx.x; i < n; i += blockDim.x) acc += samples[(size_t)i * 16 + 12];
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		acc += samples[(size_t)i * 16 + 12];
 	red[threadIdx.x] = acc;
 	__syncthreads();
 	for (int w = 128; w > 0; w >>= 1) {
 		if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
 		__syncthreads();
 	}
-	if (threadIdx.x == 0) *out = red[0] > 0.f ? (float)n / red[0] : 0.f;
+	if (threadIdx.x == 0) atomicAdd(out, red[0]);
 }
 
 are_status bad(const std::string &m) {
@@ -813,7 +816,7 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 	const float *wdev = nullptr;
 	float wscale = wmean > 0.f ? 1.0f / wmean : 0.f;
 	if (wmean < 0.f) {
-		k_weight_scale<<<1, 256, 0, s>>>(d_samples, n, grad + GN_PARAMS + 2);
+		k_weight_sum<<<std::max(1, std::min(n_sms, (n + 255) / 256)), 256, 0, s>>>(d_samples, n, grad + GN_PARAMS + 2);
 		wdev = grad + GN_PARAMS + 2;
 	}
 	k_guide_fwdbwd<<<grid, GT, guide_train_smem(), s>>>(img, bias, d_samples, n, wscale, wdev, weight_clip, loss_scale,

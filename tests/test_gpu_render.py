@@ -100,3 +100,18 @@ def test_render_argument_errors(gpu_lib):
         assert e.value.status == 1
     with pytest.raises(are.AreError):
         sc.render(dict(cam, vfov_deg=0.0), par)
+
+
+def test_tail_kernel_leaves_the_image_unchanged(gpu_lib):
+    """Random spheres (glass and metal: long paths): the tail kernel takes
+    over at different points for different pool sizes, and the image is the
+    same bit for bit."""
+    s, cam, par = small(are.CONFIG_RANDOM_SPHERES, 96, 54, 16)
+    sc = are.Scene(s)
+    n = 96 * 54 * 16
+    a, va, sa = sc.render(cam, dict(par, pool_size=4096, chunk=1))
+    b, vb, sb = sc.render(cam, dict(par, pool_size=n, chunk=1))
+    assert sa["aux"][0] > 0  # tail segments
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["samples"] == sb["samples"] == n and sa["segments"] == sb["segments"]
