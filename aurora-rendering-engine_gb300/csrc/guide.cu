@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__r
 		mbar_arrive_expect_tx(&bar[0], (uint32_t)(TC_HALVES * 2));
 		bulk_g2s(smem, tc_img, (uint32_t)(TC_HALVES * 2), &bar[0]);
 	}
-	if (!mbar_wait(&bar[0], 0, TC_POLL_LIMIT)) fail[wg] = 1;
+	if (lt == 0 && !mbar_wait(&bar[0], 0, TC_POLL_LIMIT)) fail[wg] = 1;
 
 	unsigned char *A = smem + TC_OFF_A + (size_t)wg * TC_A_BYTES;
 	const uint32_t a_addr = smem_addr(A), w_addr = smem_addr(smem);
@@ -293,9 +293,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__r
 		}
 		return true;
 	};
+	// one thread polls the mbarrier; the others sleep in the named barrier
+	// instead of spending issue slots the other warpgroups could use
 	auto wait_mma = [&]() {
-		if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+		if (lt == 0) {
+			if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+			tc_fence_before();
+		}
 		phase ^= 1u;
+		named_bar(bar_id, 128);
 		tc_fence_after();
 	};
 	named_bar(bar_id, 128);
@@ -360,10 +366,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__r
 			float o[5 * GN_LOBES];
 #pragma unroll
 			for (int col = 0; col < 5 * GN_LOBES; ++col) o[col] = __uint_as_float(r[col >> 4][col & 15]);
-			Mixture M;
-			to_mixture(o, M);
 			float pk[GN_OUT];
-			store_mixture(M, pk);
+			pack_mixture_fast(o, pk);
 			float4 *dst = reinterpret_cast<float4 *>(out + (size_t)row * GN_OUT);
 #pragma unroll
 			for (int q = 0; q < GN_OUT / 4; ++q) dst[q] = make_float4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);

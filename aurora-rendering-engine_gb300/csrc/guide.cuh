@@ -187,25 +187,43 @@ __device__ __forceinline__ void to_mixture(const float *o, Mixture &m) {
 	for (int l = 0; l < GN_LOBES; ++l) m.pi[l] *= iz;
 }
 
-// The packed form the inference kernel writes for rendering (48 floats per
-// row): lobe l's (mu.x, mu.y, mu.z, kappa) at 4 l, then (pi_l, norm_l) at
-// 32 + 2 l.
-// The mean directions are stored at unit length (to_mixture divides by
-// |m| + 1e-6): mixture_sample draws around a unit axis, so the density the
-// renderer reports is then exactly the density it samples.
-__device__ __forceinline__ void store_mixture(const Mixture &m, float *o) {
+// The packed form the inference kernel writes for rendering, 48 floats per
+// row: lobe l's (mu.x, mu.y, mu.z, kappa) at 4 l, then (pi_l, norm_l) at
+// 32 + 2 l.  The mean directions are stored at unit length (the network's
+// spec divides by |m| + 1e-6): the sampler draws around a unit axis, so the
+// density the renderer reports is exactly the density it samples.  Computed
+// with the special-function unit's exp/log and reciprocal square roots: the
+// renderer needs a density and a sampler that agree with each other (both
+// read these stored values), not the oracle's last bit.
+__device__ __forceinline__ void pack_mixture_fast(const float *o, float *pk) {
+	float mx = -1e30f;
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) mx = fmaxf(mx, o[5 * l + 4]);
+	float pi[GN_LOBES], z = 0.f;
 #pragma unroll
 	for (int l = 0; l < GN_LOBES; ++l) {
-		const f3 a = m.mu[l];
-		const float len2 = a.x * a.x + a.y * a.y + a.z * a.z;
-		const f3 u = len2 > 0.f ? scl(a, rsqrtf(len2)) : f3{ 0.f, 0.f, 1.f };
-		const float r = rsqrtf(u.x * u.x + u.y * u.y + u.z * u.z);  // a second pass: unit within an ulp or two
-		o[4 * l] = u.x * r, o[4 * l + 1] = u.y * r, o[4 * l + 2] = u.z * r, o[4 * l + 3] = m.kappa[l];
-		o[32 + 2 * l] = m.pi[l], o[33 + 2 * l] = m.norm[l];
+		const float ax = o[5 * l], ay = o[5 * l + 1], az = o[5 * l + 2];
+		const float len2 = ax * ax + ay * ay + az * az;
+		float ux = 0.f, uy = 0.f, uz = 1.f;
+		if (len2 > 0.f) {
+			const float r = rsqrtf(len2);
+			ux = ax * r, uy = ay * r, uz = az * r;
+			const float r2 = rsqrtf(ux * ux + uy * uy + uz * uz);  // a second pass: unit within an ulp or two
+			ux *= r2, uy *= r2, uz *= r2;
+		}
+		const float x = o[5 * l + 3];
+		const float k = (x > 15.f ? x : __logf(1.f + __expf(x))) + 0.05f;
+		pk[4 * l] = ux, pk[4 * l + 1] = uy, pk[4 * l + 2] = uz, pk[4 * l + 3] = k;
+		pk[33 + 2 * l] = k * __frcp_rn(6.28318530717958647692f * (1.f - __expf(-2.f * k)));
+		pi[l] = __expf(o[5 * l + 4] - mx);
+		z += pi[l];
 	}
+	const float iz = __frcp_rn(z);
+#pragma unroll
+	for (int l = 0; l < GN_LOBES; ++l) pk[32 + 2 * l] = pi[l] * iz;
 }
 
-// Density and sampling of the packed mixture (store_mixture), read lobe by
+// Density and sampling of the packed mixture (pack_mixture_fast), read lobe by
 // lobe from memory so a shading thread does not hold the whole mixture in
 // registers.  Sampling picks a lobe by its weight, then draws the vMF sample
 // of W. Jakob's stable form, cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) /

@@ -48,7 +48,7 @@ struct GuideNet {
 	are_status ensure_train(int n);
 	// n_dev: optional device row count (rows = min(n, *n_dev)), read when the kernel runs
 	// d_err: device error word to OR failures into (default: err_word)
-	// mixture_out: write the packed vMF mixture (store_mixture) instead of the raw outputs
+	// mixture_out: write the packed vMF mixture (pack_mixture_fast) instead of the raw outputs
 	are_status infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev = nullptr,
 		unsigned *d_err = nullptr, bool mixture_out = false);
 	// wmean < 0: normalise the weights by their batch mean computed on the device
