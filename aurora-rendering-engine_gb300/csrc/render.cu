@@ -370,11 +370,13 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	float *d_var = d_rgb + 3 * (size_t)W.npix;
 	const bool dev_out = (p.flags & ARE_FLAG_DEVICE_OUTPUT) != 0;
 
-	cudaEvent_t ev0, ev1;
-	cudaEventCreate(&ev0);
-	cudaEventCreate(&ev1);
-	std::vector<cudaEvent_t> kev(4 * GRAPH_ITERS);
-	for (auto &e : kev) cudaEventCreate(&e);
+	// timing events: ev0, ev1 around the render, then 4 per graph iteration (created once per scene)
+	if (sc->render_events.empty()) {
+		sc->render_events.resize(2 + 4 * GRAPH_ITERS);
+		for (auto &e : sc->render_events) cudaEventCreate(&e);
+	}
+	cudaEvent_t ev0 = sc->render_events[0], ev1 = sc->render_events[1];
+	cudaEvent_t *kev = sc->render_events.data() + 2;
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	are_status st = ARE_OK;
@@ -414,7 +416,21 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
 	}
-	if (!st) st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+	if (!st && sc->render_exec) {
+		// same kernels and events as the cached graph: update its parameters in place
+		cudaGraphExecUpdateResultInfo info;
+		if (cudaGraphExecUpdate(sc->render_exec, graph, &info) == cudaSuccess) {
+			exec = sc->render_exec;
+		} else {
+			cudaGetLastError();
+			cudaGraphExecDestroy(sc->render_exec);
+			sc->render_exec = nullptr;
+		}
+	}
+	if (!st && !exec) {
+		st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+		if (!st) sc->render_exec = exec;
+	}
 	// run until no ray is queued; counters are read back one launch behind
 	const int64_t max_launches = (int64_t)(W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk + 16;
 	int64_t g = 0;
@@ -472,11 +488,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	}
 	float total_ms = 0.f;
 	cudaEventElapsedTime(&total_ms, ev0, ev1);
-	if (exec) cudaGraphExecDestroy(exec);
-	if (graph) cudaGraphDestroy(graph);
-	for (auto &e : kev) cudaEventDestroy(e);
-	cudaEventDestroy(ev0);
-	cudaEventDestroy(ev1);
+	if (graph) cudaGraphDestroy(graph);  // the instantiated graph stays with the scene
 	if (!st && herr) {
 		set_error("device error word " + std::to_string(herr));
 		st = ARE_ERR_INTERNAL;

@@ -351,6 +351,8 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 
 are_scene::~are_scene() {
 	if (stream) cudaStreamSynchronize(stream);
+	if (render_exec) cudaGraphExecDestroy(render_exec);
+	for (cudaEvent_t e : render_events) cudaEventDestroy(e);
 	for (void *p : allocations) cudaFree(p);
 	if (ws) cudaFree(ws);
 	if (items) cudaFree(items);

@@ -28,6 +28,12 @@ struct are_scene {
 	size_t items_bytes = 0;
 	unsigned *host_counters = nullptr;  // pinned
 
+	// the render's CUDA graph and timing events, kept between renders: a new
+	// render updates the instantiated graph in place (same topology, new
+	// kernel parameters) instead of instantiating it again
+	cudaGraphExec_t render_exec = nullptr;
+	std::vector<cudaEvent_t> render_events;
+
 	~are_scene();
 };
 

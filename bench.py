@@ -241,7 +241,9 @@ def run_batch(args, rank, world) -> None:
     wl = are.batch_workload(n_scenes=64, seed=2026)
     arrays = [a for a, _, _ in wl]
     cams = [c for _, c, _ in wl]
-    params = [dict(p, seed=p["seed"] + 17 * rank) for _, _, p in wl]
+    # --spp caps every scene's samples per pixel (small profiling cases)
+    params = [dict(p, seed=p["seed"] + 17 * rank, spp=min(p["spp"], args.spp) if args.spp > 0 else p["spp"])
+              for _, _, p in wl]
     t = time.perf_counter()
     best, tuned_ms = are.batch_autotune(arrays, cams, params, calib_spp=2)
     tune_s = time.perf_counter() - t

@@ -38,6 +38,20 @@ def test_guided_is_unbiased(gpu_lib):
 
 
 @pytest.mark.skipif(not REF.exists(), reason="FP64 reference not generated")
+def test_mix_zero_is_the_plain_estimator(gpu_lib):
+    """With mix = 0 every guided vertex samples the cosine lobe with the same
+    random numbers, and the MIS weight is exactly 1: the image is the plain
+    estimator's bit for bit, whatever the network holds."""
+    s, cam, par = c4(64, 64, seed=21)
+    sc = are.Scene(s)
+    g = are.Guide(seed=4)
+    gi, gv, st = sc.render_guided(g, cam, par, are.GuideParams.make(mix=0.0, guide_depth=4, train=0))
+    pi, pv, _ = sc.render(cam, par)
+    assert st["guided_vertices"] > 0
+    assert np.array_equal(gi.view(np.uint32), pi.view(np.uint32))
+    assert np.array_equal(gv.view(np.uint32), pv.view(np.uint32))
+
+
 def test_guided_beats_plain_at_equal_samples(gpu_lib):
     r = np.load(REF)
     ref = r["mean"].astype(np.float64)
