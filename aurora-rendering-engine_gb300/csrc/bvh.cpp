@@ -5,11 +5,14 @@
 #include "bvh.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <limits>
 #include <numeric>
+#include <atomic>
+#include <thread>
 
 #include "core.h"
 
@@ -41,21 +44,62 @@ struct Builder {
 
 	Builder(const std::vector<PrimBox> &b, int leaf) : boxes(b), leaf_size(leaf) {}
 
+	// Splits [first, first + count) into chunks run on threads when the range
+	// is large (the top levels of the tree); fn(begin, end, chunk) fills
+	// chunk-local results that the caller merges with order-free operations
+	// (min, max, sums of integers), so the result does not depend on timing.
+	static constexpr int32_t PAR_RANGE = 1 << 17;
+	template <class F>
+	static int chunked(int32_t first, int32_t count, F fn) {
+		if (count < PAR_RANGE) {
+			fn(first, first + count, 0);
+			return 1;
+		}
+		static const int hw = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+		const int nc = std::min(hw, (int)(count / (PAR_RANGE / 4)));
+		if (nc <= 1) {
+			fn(first, first + count, 0);
+			return 1;
+		}
+		std::vector<std::thread> pool;
+		for (int c = 1; c < nc; ++c)
+			pool.emplace_back(fn, first + (int32_t)((int64_t)count * c / nc), first + (int32_t)((int64_t)count * (c + 1) / nc), c);
+		fn(first, first + (int32_t)(count / nc), 0);
+		for (std::thread &t : pool) t.join();
+		return nc;
+	}
+
 	void bounds(int32_t first, int32_t count, double lo[3], double hi[3], double clo[3], double chi[3]) const {
+		struct Part {
+			double lo[3], hi[3], clo[3], chi[3];
+		};
+		Part part[32];
+		const int nc = chunked(first, count, [&](int32_t b0, int32_t b1, int c) {
+			Part &q = part[c];
+			for (int k = 0; k < 3; ++k) {
+				q.lo[k] = q.clo[k] = std::numeric_limits<double>::infinity();
+				q.hi[k] = q.chi[k] = -std::numeric_limits<double>::infinity();
+			}
+			for (int32_t i = b0; i < b1; ++i) {
+				const PrimBox &b = boxes[idx[i]];
+				for (int k = 0; k < 3; ++k) {
+					q.lo[k] = std::min(q.lo[k], b.lo[k]);
+					q.hi[k] = std::max(q.hi[k], b.hi[k]);
+					double cc = cen[3 * idx[i] + k];
+					q.clo[k] = std::min(q.clo[k], cc);
+					q.chi[k] = std::max(q.chi[k], cc);
+				}
+			}
+		});
 		for (int k = 0; k < 3; ++k) {
 			lo[k] = clo[k] = std::numeric_limits<double>::infinity();
 			hi[k] = chi[k] = -std::numeric_limits<double>::infinity();
 		}
-		for (int32_t i = first; i < first + count; ++i) {
-			const PrimBox &b = boxes[idx[i]];
+		for (int c = 0; c < nc; ++c)
 			for (int k = 0; k < 3; ++k) {
-				lo[k] = std::min(lo[k], b.lo[k]);
-				hi[k] = std::max(hi[k], b.hi[k]);
-				double c = cen[3 * idx[i] + k];
-				clo[k] = std::min(clo[k], c);
-				chi[k] = std::max(chi[k], c);
+				lo[k] = std::min(lo[k], part[c].lo[k]), hi[k] = std::max(hi[k], part[c].hi[k]);
+				clo[k] = std::min(clo[k], part[c].clo[k]), chi[k] = std::max(chi[k], part[c].chi[k]);
 			}
-		}
 	}
 
 	// returns the split position (index in [first, first+count)) or -1 for a leaf
@@ -91,11 +135,30 @@ struct Builder {
 			int b = (int)((cen[3 * p + axis] - clo[axis]) * scale);
 			return std::min(std::max(b, 0), NBINS - 1);
 		};
-		for (int32_t i = first; i < first + count; ++i) {
-			Bin &b = bins[bin_of(idx[i])];
-			const PrimBox &pb = boxes[idx[i]];
-			for (int k = 0; k < 3; ++k) b.lo[k] = std::min(b.lo[k], pb.lo[k]), b.hi[k] = std::max(b.hi[k], pb.hi[k]);
-			++b.n;
+		// chunk-local bins: on the stack for one chunk, on the heap for the few large ranges
+		std::array<Bin, NBINS> local_bins;
+		std::vector<std::array<Bin, NBINS>> heap_bins(count >= PAR_RANGE ? 32 : 0);
+		auto bins_of = [&](int c) -> std::array<Bin, NBINS> & { return heap_bins.empty() ? local_bins : heap_bins[c]; };
+		const int nc = chunked(first, count, [&](int32_t b0, int32_t b1, int c) {
+			std::array<Bin, NBINS> &lb = bins_of(c);
+			for (auto &b : lb) {
+				for (int k = 0; k < 3; ++k) b.lo[k] = std::numeric_limits<double>::infinity(), b.hi[k] = -b.lo[k];
+				b.n = 0;
+			}
+			for (int32_t i = b0; i < b1; ++i) {
+				Bin &b = lb[bin_of(idx[i])];
+				const PrimBox &pb = boxes[idx[i]];
+				for (int k = 0; k < 3; ++k) b.lo[k] = std::min(b.lo[k], pb.lo[k]), b.hi[k] = std::max(b.hi[k], pb.hi[k]);
+				++b.n;
+			}
+		});
+		for (int c = 0; c < nc; ++c) {
+			const std::array<Bin, NBINS> &cb = bins_of(c);
+			for (int b = 0; b < NBINS; ++b) {
+				for (int k = 0; k < 3; ++k)
+					bins[b].lo[k] = std::min(bins[b].lo[k], cb[b].lo[k]), bins[b].hi[k] = std::max(bins[b].hi[k], cb[b].hi[k]);
+				bins[b].n += cb[b].n;
+			}
 		}
 		double right_area[NBINS];
 		int32_t right_n[NBINS];
@@ -147,30 +210,84 @@ struct Builder {
 		std::vector<Job> stack;
 		nodes.push_back(TmpNode{});
 		stack.push_back({ 0, 0, n, 0 });
+		// Large subtrees are split here; subtrees below par_min primitives are
+		// set aside and built by worker threads, each into its own node list,
+		// then appended.  Every split depends only on the subtree's own
+		// primitives, so the tree is the one a single thread would build.
+		const int32_t par_min = std::max<int32_t>(4096, n / 256);
+		std::vector<Job> deferred;
 		while (!stack.empty()) {
 			Job j = stack.back();
 			stack.pop_back();
-			double lo[3], hi[3], clo[3], chi[3];
-			bounds(j.first, j.count, lo, hi, clo, chi);
-			TmpNode &t = nodes[j.node];
-			std::memcpy(t.lo, lo, sizeof lo);
-			std::memcpy(t.hi, hi, sizeof hi);
-			t.depth = j.depth;
-			max_depth = std::max(max_depth, j.depth);
-			int32_t mid = split(j.first, j.count, j.depth, lo, hi, clo, chi);
-			if (mid < 0) {
-				nodes[j.node].first = j.first;
-				nodes[j.node].count = j.count;
+			if (j.count < par_min && j.count > leaf_size) {
+				deferred.push_back(j);
 				continue;
 			}
-			int32_t l = (int32_t)nodes.size();
-			nodes.push_back(TmpNode{});
-			nodes.push_back(TmpNode{});
-			nodes[j.node].left = l;
-			nodes[j.node].right = l + 1;
-			stack.push_back({ l + 1, mid, j.first + j.count - mid, j.depth + 1 });
-			stack.push_back({ l, j.first, mid - j.first, j.depth + 1 });
+			expand(j, nodes, stack, max_depth);
 		}
+		if (deferred.empty()) return;
+		std::vector<std::vector<TmpNode>> local(deferred.size());
+		std::vector<int> local_depth(deferred.size(), 0);
+		std::atomic<size_t> next_job{ 0 };
+		auto worker = [&]() {
+			for (size_t k; (k = next_job.fetch_add(1)) < deferred.size();) {
+				std::vector<TmpNode> &ln = local[k];
+				std::vector<Job> st;
+				ln.push_back(TmpNode{});
+				st.push_back({ 0, deferred[k].first, deferred[k].count, deferred[k].depth });
+				while (!st.empty()) {
+					Job j = st.back();
+					st.pop_back();
+					expand(j, ln, st, local_depth[k]);
+				}
+			}
+		};
+		const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+		const unsigned nthreads = (unsigned)std::min<size_t>(hw, deferred.size());
+		std::vector<std::thread> pool;
+		for (unsigned t = 1; t < nthreads; ++t) pool.emplace_back(worker);
+		worker();
+		for (std::thread &t : pool) t.join();
+		// append each subtree: local node 0 fills the placeholder, the rest shift by base - 1
+		for (size_t k = 0; k < deferred.size(); ++k) {
+			const std::vector<TmpNode> &ln = local[k];
+			const int32_t base = (int32_t)nodes.size();
+			auto map = [&](int32_t i) { return i < 0 ? i : base + i - 1; };
+			TmpNode root = ln[0];
+			root.left = map(root.left), root.right = map(root.right);
+			nodes[deferred[k].node] = root;
+			for (size_t i = 1; i < ln.size(); ++i) {
+				TmpNode t = ln[i];
+				t.left = map(t.left), t.right = map(t.right);
+				nodes.push_back(t);
+			}
+			max_depth = std::max(max_depth, local_depth[k]);
+		}
+	}
+
+	// one step of the build: bounds and split of job j's range into node j.node of `ns`
+	template <class JobT>
+	void expand(const JobT &j, std::vector<TmpNode> &ns, std::vector<JobT> &stack, int &depth_max) {
+		double lo[3], hi[3], clo[3], chi[3];
+		bounds(j.first, j.count, lo, hi, clo, chi);
+		TmpNode &t = ns[j.node];
+		std::memcpy(t.lo, lo, sizeof lo);
+		std::memcpy(t.hi, hi, sizeof hi);
+		t.depth = j.depth;
+		depth_max = std::max(depth_max, j.depth);
+		int32_t mid = split(j.first, j.count, j.depth, lo, hi, clo, chi);
+		if (mid < 0) {
+			ns[j.node].first = j.first;
+			ns[j.node].count = j.count;
+			return;
+		}
+		int32_t l = (int32_t)ns.size();
+		ns.push_back(TmpNode{});
+		ns.push_back(TmpNode{});
+		ns[j.node].left = l;
+		ns[j.node].right = l + 1;
+		stack.push_back({ l + 1, mid, j.first + j.count - mid, j.depth + 1 });
+		stack.push_back({ l, j.first, mid - j.first, j.depth + 1 });
 	}
 };
 
