@@ -43,7 +43,6 @@ struct GuidedState {
 	GuideBox box;
 	float mix;
 	int guide_depth;
-	float rr_clip;
 };
 
 // Closest hits of the queued rays (as k_intersect), then the network's input
