@@ -33,6 +33,7 @@ EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
 FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
 CONFIG_SPHERE_FIELD = 6
+SCHEDULE_AUTO, SCHEDULE_WAVEFRONT, SCHEDULE_MEGAKERNEL = 0, 1, 2
 TONEMAP_GAMMA, TONEMAP_LINEAR = 0, 1
 
 MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("texture", "<i4"), ("fuzz", "<f4"), ("ior", "<f4"),
@@ -164,7 +165,7 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("seed", C.c_uint64), ("rr_depth", C.c_int32), ("t_min", C.c_float), ("estimator", C.c_int32),
                 ("flags", C.c_int32), ("pool_size", C.c_int32), ("chunk", C.c_int32), ("block_size", C.c_int32),
-                ("reserved_", C.c_int32)]
+                ("schedule", C.c_int32)]
 
     def to_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -12,6 +12,8 @@
 //
 // The scratch — the path pool, its queues and accumulators, and one work
 // item per pixel — lives in g_noalloc_scratch below (ARE_NOALLOC_SCRATCH_BYTES).
+// Both schedules of are_render run here (params->schedule; the megakernel is
+// one launch of k_tail with at most ARE_NOALLOC_MAX_PATHS paths).
 // The array belongs to the library's device module: every GPU that loads the
 // library holds it until the process exits.  Kernels receive its address; host
 // code never dereferences the symbol (on the host, the name is only a
@@ -101,7 +103,11 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 		return bad("pool_size above ARE_NOALLOC_MAX_PATHS (" + std::to_string(ARE_NOALLOC_MAX_PATHS) + ")");
 	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");
 	if (!(p.t_min >= 0.0f) || !std::isfinite(p.t_min)) return bad("t_min must be finite and >= 0");
+	if (p.schedule < ARE_SCHEDULE_AUTO || p.schedule > ARE_SCHEDULE_MEGAKERNEL) return bad("unknown schedule");
 	if (cudaSetDevice(sc->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
+	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const int g_tail = tail_grid(linear, sc->n_sms);
 	unsigned char *base = nullptr;
 	if (are_status st = scratch_address(sc->device, &base)) return st;
 
@@ -112,7 +118,8 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	W.chunk = p.spp;
 	W.nchunk = 1;
 	W.n_items = W.npix;
-	int P = p.pool_size > 0 ? p.pool_size : ARE_NOALLOC_MAX_PATHS;
+	// megakernel: at most one path per resident thread of its persistent grid
+	int P = p.pool_size > 0 ? p.pool_size : mega ? std::min(ARE_NOALLOC_MAX_PATHS, g_tail * BLOCK) : ARE_NOALLOC_MAX_PATHS;
 	P = (int)std::min<int64_t>(P, W.n_items);
 	P = std::min((P + 31) & ~31, ARE_NOALLOC_MAX_PATHS);
 	W.P = P;
@@ -153,10 +160,16 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_init launch");
 	}
+	if (!st && mega) {
+		// the whole render in one persistent launch (queue 0 holds one camera path per thread)
+		launch_tail(linear, g_tail, s, sc->dev, W);
+		++launches[ARE_KERNEL_OTHER];
+		st = cuda_status(cudaGetLastError(), "k_tail launch");
+	}
 	const int g_int = blocks_for((const void *)k_intersect, sc->n_sms);
 	const int g_sh = blocks_for((const void *)k_shade, sc->n_sms);
 	const int64_t max_rounds = (W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk / GRAPH_ITERS + 16;
-	for (int64_t round = 0; !st; ++round) {
+	for (int64_t round = 0; !st && !mega; ++round) {
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
 			int par = it & 1;
 			k_intersect<<<g_int, BLOCK, 0, s>>>(sc->dev, W, par);

@@ -41,17 +41,16 @@ __device__ __forceinline__ void put_camera_ray(const Wave &W, int q, unsigned po
 	W.qd[q][pos] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// Kahan accumulation of a finished path's radiance L into its slot, in sample
-// order; when the slot's work item is complete its sums are published and the
-// slot takes the next item from *next_item.  Returns whether the slot has a
-// next sample (item, j).
-__device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64_t &item, int &j, uint32_t &err,
-	unsigned *next_item) {
+// Kahan accumulation of a finished path's radiance L into a slot's sums (sm,
+// compensation cm, sum of squares q), in sample order; when the slot's work
+// item is complete its sums are published and the slot takes the next item
+// from *next_item.  Returns whether the slot has a next sample (item, j).
+__device__ __forceinline__ bool accumulate(const Wave &W, f3 L, int64_t &item, int &j, uint32_t &err,
+	unsigned *next_item, float4 &sm, float4 &cm, float4 &q) {
 	if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) {
 		err |= ERR_NONFINITE;
 		L = f3{ 0.f, 0.f, 0.f };
 	}
-	float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
 	float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
 	float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
 	cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
@@ -67,10 +66,18 @@ __device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64
 		item = (int64_t)atomicAdd(next_item, 1u);
 		j = 0;
 	}
+	return item < W.n_items;
+}
+
+// accumulate() on the slot's sums in device memory
+__device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64_t &item, int &j, uint32_t &err,
+	unsigned *next_item) {
+	float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
+	const bool more = accumulate(W, L, item, j, err, next_item, sm, cm, q);
 	W.acc_s[slot] = sm;
 	W.acc_c[slot] = cm;
 	W.acc_q[slot] = q;
-	return item < W.n_items;
+	return more;
 }
 
 // A path between bounces: its ray and the state that travels with it.

@@ -18,7 +18,8 @@
 // slot in order, so the per-item Kahan sums - and the image - do not depend
 // on scheduling.  `resolve` adds the items of each pixel in chunk order.
 // Iterations are captured K at a time in a CUDA graph; when every item is
-// taken and few paths remain, `tail` finishes them in one launch.
+// taken and few paths remain, `tail` finishes them in one launch.  Under the
+// megakernel schedule `tail` renders the whole frame in one persistent launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -109,9 +110,12 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 
 // One bounce of path P at hit h (t, leaf bits, u, v): scatter and, when the
 // path ends, the accumulate step and the slot's next camera path.  Returns
-// true if P holds a ray to trace (the continued path or the new one).
+// true if P holds a ray to trace (the continued path or the new one).  With
+// ACC_IN_REGS the slot's sums are the caller's registers (sm, cm, q), else
+// they are read and written in device memory.
+template <bool ACC_IN_REGS>
 __device__ __forceinline__ bool shade_step(const DevScene &S, const Wave &W, PathState &P, float4 h, uint32_t &err,
-	unsigned long long &done) {
+	unsigned long long &done, float4 &sm, float4 &cm, float4 &q) {
 	bool cont = false;
 	const int leaf = __float_as_int(h.y);
 	if (leaf < 0) {
@@ -134,7 +138,9 @@ __device__ __forceinline__ bool shade_step(const DevScene &S, const Wave &W, Pat
 	++done;
 	int64_t item = P.item;
 	int j = P.j;
-	if (!finish_path(W, P.slot, P.L, item, j, err, &W.cnt[3])) return false;
+	const bool more = ACC_IN_REGS ? accumulate(W, P.L, item, j, err, &W.cnt[3], sm, cm, q)
+								  : finish_path(W, P.slot, P.L, item, j, err, &W.cnt[3]);
+	if (!more) return false;
 	camera_path(W, P.slot, item, j, P);
 	return true;
 }
@@ -155,7 +161,8 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 		PathState P;
 		if (i < n) {
 			P = load_path(W, par, i);
-			live = shade_step(S, W, P, W.hit[i], err, done);
+			float4 unused;
+			live = shade_step<false>(S, W, P, W.hit[i], err, done, unused, unused, unused);
 		}
 		unsigned pos = warp_append(&W.cnt[out], live);
 		if (live) {
@@ -171,18 +178,26 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 	if (err) atomicOr(&W.cnt[4], err);
 }
 
-// The end of a render, when every work item has been taken and few paths are
-// left: one thread per queued path traces it to the end, then the rest of
-// its slot's samples, with the same device functions and in the same sample
-// order as the wavefront, so the image is the same bit for bit.  It replaces
-// the long tail of nearly empty wavefront iterations (paths that keep
-// bouncing between glass and metal).
-__global__ void __launch_bounds__(BLOCK) k_tail(DevScene S, Wave W, int par) {
+// One thread per queued path traces it to the end, then the rest of its
+// slot's samples and, while work items are left, the next ones, with the same
+// device functions and in the same sample order as the wavefront, so the image
+// is the same bit for bit.  Two uses: the end of a wavefront render, when
+// every item has been taken and few paths are left (it replaces the long tail
+// of nearly empty iterations: paths that keep bouncing between glass and
+// metal), and the whole render under the megakernel schedule (queue 0 then
+// holds one camera path per resident thread).
+//
+// One instantiation per closest-hit strategy (LINEAR: the staged linear scan of
+// a scene with at most LINEAR_MAX primitives, else the BVH), each with the
+// occupancy that measured fastest for it.
+template <bool LINEAR>
+__global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
+	k_tail(DevScene S, Wave W, int par) {
 	__shared__ float4 snodes[2 * SMEM_NODES];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
-	const bool linear = S.n_prims <= LINEAR_MAX;
+	constexpr bool linear = LINEAR;
 	if (linear) {
 		stage_prims(S, snodes);
 		__syncthreads();
@@ -194,13 +209,18 @@ __global__ void __launch_bounds__(BLOCK) k_tail(DevScene S, Wave W, int par) {
 	const float inf = __int_as_float(0x7f800000);
 	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		PathState P = load_path(W, par, i);
+		const int slot = P.slot;
+		// the slot's sums stay in registers while this thread owns the slot
+		float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
 		bool live = true;
 		while (live) {
 			Hit hh = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf)
 							: closest_hit(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err);
 			++segments;
-			live = shade_step(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done);
+			live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
+				cm, q);
 		}
+		W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 	}
 	for (int o = 16; o > 0; o >>= 1) {
 		done += __shfl_down_sync(0xffffffffu, done, o);
@@ -290,6 +310,17 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) 
 	f.height = h;
 }
 
+void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W) {
+	if (linear)
+		k_tail<true><<<grid, BLOCK, 0, s>>>(S, W, 0);
+	else
+		k_tail<false><<<grid, BLOCK, 0, s>>>(S, W, 0);
+}
+
+int tail_grid(bool linear, int n_sms) {
+	return grid_for(linear ? (const void *)k_tail<true> : (const void *)k_tail<false>, n_sms);
+}
+
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *prm, float *rgb, float *var,
 	are_render_stats *stats) {
 	if (!sc || !cam || !prm || !rgb) return bad("null scene, camera, params or output");
@@ -303,15 +334,27 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	if (p.estimator == ARE_EST_LEGACY_RT) return render_legacy(sc, cam, p, rgb, stats);
 	if (p.estimator != ARE_EST_PATH) return bad("unknown estimator");
 
+	if (p.schedule < ARE_SCHEDULE_AUTO || p.schedule > ARE_SCHEDULE_MEGAKERNEL) return bad("unknown schedule");
+	// measured on GB300, the megakernel is the faster schedule on every workload scene (the path
+	// state stays in registers; no queue records go through memory between bounces)
+	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
+	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
+	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
+	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const int g_tail = tail_grid(linear, sc->n_sms);
+
 	Wave W{};
 	W.npix = p.width * p.height;
 	W.spp = p.spp;
 	int64_t total = (int64_t)W.npix * p.spp;
-	int P = p.pool_size > 0 ? p.pool_size : (1 << 20);
+	// megakernel: one path per resident thread of the persistent launch
+	int P = p.pool_size > 0 ? p.pool_size : mega ? g_tail * BLOCK : (1 << 20);
 	if (P > (1 << 24)) return bad("pool_size too large (max 2^24)");
 	int chunk = p.chunk;
-	// small work items keep the end-of-frame tail short (a slot finishes its item before going idle)
-	if (chunk <= 0) chunk = (int)std::min<int64_t>(16, std::max<int64_t>(1, total / (16 * (int64_t)P)));
+	// small work items keep the end-of-frame tail short (a slot finishes its item before going idle),
+	// large ones take fewer atomics on the next-item counter
+	if (chunk <= 0)
+		chunk = (int)std::min<int64_t>(16, std::max<int64_t>(1, total / ((mega ? 64 : 16) * (int64_t)P)));
 	chunk = std::min(chunk, p.spp);
 	W.chunk = chunk;
 	W.nchunk = (p.spp + chunk - 1) / chunk;
@@ -384,9 +427,6 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	int64_t launches[4] = { 0, 0, 0, 0 };
 	double kms[4] = { 0.0, 0.0, 0.0, 0.0 };
 
-	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
-	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
-	const int g_tail = grid_for((const void *)k_tail, sc->n_sms);
 	// queued paths below which the tail kernel takes over (once every item is taken): its time is set
 	// by the longest remaining path, not by how many paths are left, so it can start early
 	const unsigned tail_max = (unsigned)std::max<int64_t>(8192, P / 4);
@@ -402,9 +442,20 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_init launch");
 	}
+	if (!st && mega) {
+		// the whole render in one persistent launch (queue 0 holds one camera path per thread)
+		cudaEventRecord(kev[0], s);
+		launch_tail(linear, g_tail, s, S, W);
+		cudaEventRecord(kev[1], s);
+		++launches[ARE_KERNEL_OTHER];
+		st = cuda_status(cudaGetLastError(), "k_tail launch");
+		if (!st) st = cuda_status(cudaStreamSynchronize(s), "render");
+		float ms = 0.f;
+		if (!st && cudaEventElapsedTime(&ms, kev[0], kev[1]) == cudaSuccess) kms[ARE_KERNEL_OTHER] += ms;
+	}
 	// capture GRAPH_ITERS iterations, each bracketed by timing events
-	if (!st) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-	if (!st) {
+	if (!st && !mega) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+	if (!st && !mega) {
 		for (int it = 0; it < GRAPH_ITERS; ++it) {
 			int par = it & 1;
 			// external event nodes: the events are recorded each time the graph runs
@@ -416,7 +467,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "cudaStreamEndCapture");
 	}
-	if (!st && sc->render_exec) {
+	if (!st && !mega && sc->render_exec) {
 		// same kernels and events as the cached graph: update its parameters in place
 		cudaGraphExecUpdateResultInfo info;
 		if (cudaGraphExecUpdate(sc->render_exec, graph, &info) == cudaSuccess) {
@@ -427,14 +478,14 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			sc->render_exec = nullptr;
 		}
 	}
-	if (!st && !exec) {
+	if (!st && !mega && !exec) {
 		st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
 		if (!st) sc->render_exec = exec;
 	}
 	// run until no ray is queued; counters are read back one launch behind
 	const int64_t max_launches = (int64_t)(W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk + 16;
 	int64_t g = 0;
-	while (!st) {
+	while (!st && !mega) {
 		st = cuda_status(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
 		if (st) break;
 		cudaMemcpyAsync(sc->host_counters, W.cnt, 8 * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
@@ -453,7 +504,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		if (sc->host_counters[3] >= W.n_items && sc->host_counters[0] <= tail_max) {
 			// every work item is taken and few paths are left: finish them in one launch
 			cudaEventRecord(kev[0], s);
-			k_tail<<<g_tail, BLOCK, 0, s>>>(S, W, 0);
+			launch_tail(linear, g_tail, s, S, W);
 			cudaEventRecord(kev[1], s);
 			st = cuda_status(cudaGetLastError(), "k_tail launch");
 			if (!st) st = cuda_status(cudaStreamSynchronize(s), "render tail");

@@ -12,6 +12,10 @@ namespace are_core {
 
 constexpr int GRAPH_ITERS = 8;  // iterations per graph launch (even)
 constexpr int BLOCK = 256;
+// resident blocks per SM requested for the tail / megakernel (registers per thread follow):
+// linear-scan scenes run best at 4 (64 registers), BVH scenes at 2 (deeper traversal state)
+constexpr int TAIL_MIN_BLOCKS_LINEAR = 4;
+constexpr int TAIL_MIN_BLOCKS_BVH = 2;
 
 struct Wave {
 	// Ray queues: one 64-byte record per queued path segment, SoA over 4 float4:
@@ -46,7 +50,10 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);
 __global__ void k_init(Wave W, int n_first);
 __global__ void k_intersect(DevScene S, Wave W, int par);
 __global__ void k_shade(DevScene S, Wave W, int par);
-__global__ void k_tail(DevScene S, Wave W, int par);
 __global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ var, int clamp);
+// k_tail (render.cu) for a scene scanned linearly (linear) or through its BVH, on queue 0;
+// tail_grid: its persistent grid (resident blocks x SMs)
+void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W);
+int tail_grid(bool linear, int n_sms);
 
 }  // namespace are_core

@@ -56,6 +56,11 @@ WORKLOAD = WORKLOADS["cornell"][1]
 BYTES_INTERSECT = 32 + 16          # per segment: ray (origin, direction) in, hit record out
 BYTES_SHADE_SEGMENT = 64 + 16 + 64  # per segment: queue record + hit in, one 64-byte record out (next ray or camera ray)
 BYTES_SHADE_SAMPLE = 48 + 48       # per sample: the slot's Kahan accumulators read and written
+# the path's algorithmic bytes as a wavefront would move them (camera ray, accumulate: 152 per sample;
+# ray 32 + hit 16 + path state and material 164 + next ray and state 48: 260 per segment); the
+# megakernel keeps all of it on chip, so its DRAM traffic is far below these
+BYTES_MEGA_SAMPLE = 152
+BYTES_MEGA_SEGMENT = 260
 
 
 def dist_env():
@@ -499,6 +504,8 @@ def main() -> None:
     ap.add_argument("--spp", type=int, default=0, help="samples per pixel (0 = the workload's own)")
     ap.add_argument("--pool", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--schedule", choices=("auto", "wavefront", "megakernel"), default="auto",
+                    help="are_render schedule (auto = megakernel)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-guiding", action="store_true", help="skip the guided-vs-plain relMSE comparison")
     ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
@@ -538,7 +545,8 @@ def main() -> None:
 
     scene_arrays = dataclasses.replace(scene_arrays, bvh_build=are.BVH_DEVICE if args.bvh == "device" else are.BVH_HOST_SAH)
     spp = args.spp if args.spp > 0 else par["spp"]
-    par = dict(par, spp=spp, pool_size=args.pool, chunk=args.chunk)
+    sched = {"auto": are.SCHEDULE_AUTO, "wavefront": are.SCHEDULE_WAVEFRONT, "megakernel": are.SCHEDULE_MEGAKERNEL}
+    par = dict(par, spp=spp, pool_size=args.pool, chunk=args.chunk, schedule=sched[args.schedule])
     W, H = par["width"], par["height"]
     samples_per_step = W * H * par["spp"]
     sc = are.Scene(scene_arrays)
@@ -573,22 +581,30 @@ def main() -> None:
     launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
     segments = sum(s["segments"] for s in stats)
     samples = sum(s["samples"] for s in stats)
-    tail_segments = sum(int(s["aux"][0]) for s in stats)  # traced by the end-of-render tail kernel ("other")
+    tail_segments = sum(int(s["aux"][0]) for s in stats)  # traced by k_tail ("other"): all of them under the megakernel
     wave_segments = segments - tail_segments
-    algo = {"intersect": BYTES_INTERSECT * wave_segments,
-            "shade": BYTES_SHADE_SEGMENT * wave_segments + BYTES_SHADE_SAMPLE * samples}
-    dom = max(("intersect", "shade"), key=lambda k: tot[k])
+    mega = launches["intersect"] == 0  # megakernel schedule: one k_tail launch per frame
     peaks = measured_peaks()
-    achieved = algo[dom] / (tot[dom] / 1e3) / 1e9
+    traffic_file = REPO / "profiles" / "traffic.json"
+    traffic = json.loads(traffic_file.read_text()) if traffic_file.exists() else {}
+    if mega:
+        dom, t_dom, n_launch = "k_tail (megakernel)", tot["other"], args.steps
+        algo_bytes = BYTES_MEGA_SAMPLE * samples + BYTES_MEGA_SEGMENT * segments
+        per_sample = traffic.get(f"megakernel_{args.workload}", {}).get("bytes_per_sample")
+        traffic_launch = round(per_sample * samples / n_launch) if per_sample is not None else None
+    else:
+        algo = {"intersect": BYTES_INTERSECT * wave_segments,
+                "shade": BYTES_SHADE_SEGMENT * wave_segments + BYTES_SHADE_SAMPLE * samples}
+        dom = max(("intersect", "shade"), key=lambda k: tot[k])
+        t_dom, n_launch, algo_bytes = tot[dom], max(1, launches[dom]), algo[dom]
+        traffic_launch = traffic.get(dom)
+    achieved = algo_bytes / (t_dom / 1e3) / 1e9
     roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
-            "bytes_per_launch": round(algo[dom] / max(1, launches[dom])),
-            "avg_launch_us": round(tot[dom] * 1e3 / max(1, launches[dom]), 2),
+            "bytes_per_launch": round(algo_bytes / n_launch),
+            "avg_launch_us": round(t_dom * 1e3 / n_launch, 2),
             "kernel_ms": {k: round(v, 2) for k, v in tot.items()},
-            "traffic": None}
-    prof = REPO / "profiles" / "traffic.json"
-    if prof.exists():
-        roof["traffic"] = json.loads(prof.read_text()).get(dom)
+            "traffic": traffic_launch}
 
     # end to end through the C ABI with host buffers
     host_rgb = np.empty(W * H * 3, np.float32)
@@ -634,8 +650,9 @@ def main() -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
                        "rr_depth": par["rr_depth"], "primitives": scene_arrays.n_prims, "bvh_build": args.bvh,
+                       "schedule": "megakernel" if mega else "wavefront",
                        "parallelism": f"replicas{world}",
-                       "l2": "flushed (256 MB write) between steps; path pool > L2"},
+                       "l2": "flushed (256 MB write) between steps"},
             "segments_per_sample": round(segments / max(1, samples), 4),
             "tail_segments_frac": round(tail_segments / max(1, segments), 5),
             "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,

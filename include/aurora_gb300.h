@@ -157,8 +157,20 @@ typedef struct are_render_params {
 	int32_t pool_size;          /* paths in flight; 0 = auto */
 	int32_t chunk;              /* samples per work item; 0 = auto */
 	int32_t block_size;         /* threads per block; 0 = auto */
-	int32_t reserved_;
+	int32_t schedule;           /* ARE_SCHEDULE_*; the image does not depend on it */
 } are_render_params;
+
+/* How are_render (ARE_EST_PATH) runs its paths.  Both produce the same image
+ * bit for bit for the same chunk (every work item's samples run in one slot,
+ * in order).
+ *   WAVEFRONT:  a pool of paths in device memory, one closest-hit and one
+ *               shading kernel per bounce over compacted queues, in CUDA graphs;
+ *   MEGAKERNEL: one persistent launch, one path per resident thread, each
+ *               thread tracing its paths to the end and taking the next work
+ *               item itself; the path state stays in registers;
+ *   AUTO:       MEGAKERNEL (the faster of the two on every scene measured).
+ * The automatic chunk differs between the two, so set chunk to compare. */
+enum { ARE_SCHEDULE_AUTO = 0, ARE_SCHEDULE_WAVEFRONT = 1, ARE_SCHEDULE_MEGAKERNEL = 2 };
 
 enum { ARE_KERNEL_INTERSECT = 0, ARE_KERNEL_SHADE = 1, ARE_KERNEL_GENERATE = 2, ARE_KERNEL_OTHER = 3 };
 
@@ -221,7 +233,7 @@ ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n,
  * capture, or a plugin host that gives a plugin a fixed device-memory budget
  * and forbids allocations of its own.  Such a caller creates the scene first
  * (are_scene_create allocates) and then calls are_render_noalloc, which
- * renders the path estimator (ARE_EST_PATH) like are_render but calls no
+ * renders the path estimator (ARE_EST_PATH, either schedule) like are_render but calls no
  * cudaMalloc, cudaFree or other allocating routine and creates no streams,
  * events or graphs.
  *

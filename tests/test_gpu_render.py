@@ -1,5 +1,5 @@
-"""Image parity on the GPU: the wavefront path tracer (are_render) against
-the oracle's CPU render of the same estimator.
+"""Image parity on the GPU: the path tracer (are_render; megakernel and
+wavefront schedules) against the oracle's CPU render of the same estimator.
 
 * same seed: both sides consume the same random numbers, so the images agree
   to float rounding except where an ulp-level difference in a transcendental
@@ -106,12 +106,58 @@ def test_tail_kernel_leaves_the_image_unchanged(gpu_lib):
     """Random spheres (glass and metal: long paths): the tail kernel takes
     over at different points for different pool sizes, and the image is the
     same bit for bit."""
-    s, cam, par = small(are.CONFIG_RANDOM_SPHERES, 96, 54, 16)
+    s, cam, par = small(are.CONFIG_RANDOM_SPHERES, 96, 54, 16, schedule=are.SCHEDULE_WAVEFRONT)
     sc = are.Scene(s)
     n = 96 * 54 * 16
     a, va, sa = sc.render(cam, dict(par, pool_size=4096, chunk=1))
     b, vb, sb = sc.render(cam, dict(par, pool_size=n, chunk=1))
+    assert sa["kernel_launches"]["intersect"] > 0  # the wavefront ran before the tail
     assert sa["aux"][0] > 0  # tail segments
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
     assert sa["samples"] == sb["samples"] == n and sa["segments"] == sb["segments"]
+
+
+@pytest.mark.parametrize("cfg,w,h,spp,chunk", [(are.CONFIG_CORNELL, 64, 64, 48, 4),           # linear scan
+                                               (are.CONFIG_RANDOM_SPHERES, 96, 54, 24, 1),   # BVH in shared memory
+                                               (are.CONFIG_CORNELL_OCCLUDED, 40, 40, 32, 16),
+                                               (are.CONFIG_LEGACY_RT, 48, 48, 16, 3)])       # rt.cpp triangles
+def test_megakernel_equals_wavefront(gpu_lib, cfg, w, h, spp, chunk):
+    """The two schedules run every work item's samples in one slot in sample
+    order with the same device functions: same chunk, same image bit for bit,
+    whatever the pool size."""
+    s, cam, par = small(cfg, w, h, spp, chunk=chunk, estimator=are.EST_PATH)
+    sc = are.Scene(s)
+    a, va, sa = sc.render(cam, dict(par, schedule=are.SCHEDULE_WAVEFRONT))
+    b, vb, sb = sc.render(cam, dict(par, schedule=are.SCHEDULE_MEGAKERNEL))
+    c, vc, sc_ = sc.render(cam, dict(par, schedule=are.SCHEDULE_MEGAKERNEL, pool_size=1024))
+    assert sa["kernel_launches"]["intersect"] > 0 and sb["kernel_launches"]["intersect"] == 0
+    for x, vx in ((b, vb), (c, vc)):
+        assert np.array_equal(a.view(np.uint32), x.view(np.uint32))
+        assert np.array_equal(va.view(np.uint32), vx.view(np.uint32))
+    assert sa["samples"] == sb["samples"] == sc_["samples"] == w * h * spp
+    assert sa["segments"] == sb["segments"] == sc_["segments"]
+    assert sb["aux"][0] == sb["segments"]  # every segment traced by the megakernel
+
+
+def test_megakernel_mesh_equals_wavefront(gpu_lib):
+    """The 2M-triangle mesh (BVH far larger than shared memory, watertight
+    triangles) at a small image: both schedules give the same bits."""
+    s, cam, par = small(are.CONFIG_MESH, 64, 36, 8, chunk=2)
+    sc = are.Scene(s)
+    a, va, sa = sc.render(cam, dict(par, schedule=are.SCHEDULE_WAVEFRONT))
+    b, vb, sb = sc.render(cam, dict(par, schedule=are.SCHEDULE_MEGAKERNEL))
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["segments"] == sb["segments"] and sa["error_word"] == sb["error_word"] == 0
+
+
+def test_schedule_argument(gpu_lib):
+    s, cam, par = small(are.CONFIG_CORNELL, 16, 16, 4)
+    sc = are.Scene(s)
+    _, _, st = sc.render(cam, par)  # automatic schedule: the megakernel
+    assert st["kernel_launches"]["intersect"] == 0 and st["kernel_launches"]["other"] == 3
+    for bad in (-1, 3):
+        with pytest.raises(are.AreError) as e:
+            sc.render(cam, dict(par, schedule=bad))
+        assert e.value.status == 1

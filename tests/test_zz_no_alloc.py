@@ -38,8 +38,10 @@ def test_noalloc_matches_are_render_twice(gpu_lib):
         s, cam, par = are.build_config(cfg)
         cases.append((are.Scene(s), cam, dict(par, width=w, height=h, spp=spp, seed=4)))
     torch.cuda.init()
-    for call in range(2):  # two calls in a row per scene, alternating scenes
+    for call, sched in enumerate((are.SCHEDULE_AUTO, are.SCHEDULE_WAVEFRONT, are.SCHEDULE_MEGAKERNEL)):
+        # calls in a row per scene, alternating scenes, through both schedules
         for sc, cam, par in cases:
+            par = dict(par, schedule=sched)
             n = par["width"] * par["height"] * 3
             rgb = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
             var = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
@@ -48,7 +50,7 @@ def test_noalloc_matches_are_render_twice(gpu_lib):
             assert status == 0, lib.are_last_error().decode()
             assert st["samples"] == par["width"] * par["height"] * par["spp"] and st["error_word"] == 0
             # the allocating entry point with the same work split (one work item per pixel)
-            ref, ref_var, _ = sc.render(cam, dict(par, chunk=par["spp"]))
+            ref, ref_var, _ = sc.render(cam, dict(par, chunk=par["spp"], schedule=are.SCHEDULE_AUTO))
             got = rgb.cpu().numpy().reshape(ref.shape)
             got_var = var.cpu().numpy().reshape(ref.shape)
             assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), f"call {call}: image differs"
