@@ -39,11 +39,16 @@ namespace are_core {
 // ---------------------------------------------------------------------------
 // batched closest hit (are_intersect)
 
+// LINEAR: a scene of at most LINEAR_MAX primitives, scanned from shared memory
+// (its instantiation holds the staged primitives and the per-warp scratch);
+// else the BVH with its top levels in shared memory.
+template <bool LINEAR>
 __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const float4 *__restrict__ rays, int64_t n,
 	float4 *__restrict__ hits, unsigned *err_word) {
-	__shared__ float4 snodes[2 * SMEM_NODES];
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	int n_snodes = 0;
-	const bool linear = S.n_prims <= LINEAR_MAX;
+	constexpr bool linear = LINEAR;
 	if (linear) {
 		stage_prims(S, snodes);
 		__syncthreads();
@@ -51,16 +56,25 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 		stage_nodes(S, snodes, n_snodes);
 	}
 	uint32_t err = 0;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+	// whole warps walk the rays together (the linear scan is warp-cooperative)
+	for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+		const int64_t i = base + threadIdx.x;
+		const bool active = i < n;
+		float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+		if (active) r0 = rays[2 * i], r1 = rays[2 * i + 1];
 		Hit h;
-		if (linear) {
+		// the cooperative scan orders hits by t's bits, which needs t > 0: rays with tmin >= 0
+		if (linear && __all_sync(0xffffffffu, !active || r0.w >= 0.0f)) {
+			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w, active,
+				scratch[threadIdx.x >> 5]);
+		} else if (linear && active) {
 			h = closest_hit_linear(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w);
-		} else {
+		} else if (active) {
 			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
 		}
-		hits[i] = h.leaf >= 0 ? make_float4(h.t, __int_as_float(h.gid), h.u, h.v)
-							  : make_float4(__int_as_float(0x7f800000), __int_as_float(-1), 0.f, 0.f);
+		if (active)
+			hits[i] = h.leaf >= 0 ? make_float4(h.t, __int_as_float(h.gid), h.u, h.v)
+								  : make_float4(__int_as_float(0x7f800000), __int_as_float(-1), 0.f, 0.f);
 	}
 	if (err) atomicOr(err_word, err);
 }
@@ -78,8 +92,10 @@ __global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
 	}
 }
 
+template <bool LINEAR>
 __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par) {
-	__shared__ float4 snodes[2 * SMEM_NODES];
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -88,7 +104,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 		atomicAdd(&W.stat[0], (unsigned long long)n);
 	}
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
-	const bool linear = S.n_prims <= LINEAR_MAX;
+	constexpr bool linear = LINEAR;
 	if (linear) {
 		stage_prims(S, snodes);
 		__syncthreads();
@@ -99,11 +115,20 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 	const float4 *__restrict__ qb = W.qb[par];
 	uint32_t err = 0;
 	const float inf = __int_as_float(0x7f800000);
-	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float4 r0 = qa[i], r1 = qb[i];
-		Hit h = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf)
-					   : closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
-		W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
+	// whole warps walk the queue together (the linear scan is warp-cooperative)
+	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		const unsigned i = base + threadIdx.x;
+		const bool active = i < n;
+		float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0;
+		if (active) r0 = qa[i], r1 = qb[i];
+		Hit h;
+		if (linear) {
+			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf, active,
+				scratch[threadIdx.x >> 5]);
+		} else if (active) {
+			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
+		}
+		if (active) W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}
 	if (err) atomicOr(&W.cnt[4], err);
 }
@@ -193,12 +218,14 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 template <bool LINEAR>
 __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
 	k_tail(DevScene S, Wave W, int par) {
-	__shared__ float4 snodes[2 * SMEM_NODES];
+	// linear scenes: the staged primitives and leaf boxes (6 float4 per primitive at most) and
+	// one closest-hit scratch per warp; BVH scenes: the top BVH levels
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
-	constexpr bool linear = LINEAR;
-	if (linear) {
+	if (LINEAR) {
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else {
@@ -207,20 +234,45 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 	uint32_t err = 0;
 	unsigned long long done = 0, segments = 0;
 	const float inf = __int_as_float(0x7f800000);
-	for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		PathState P = load_path(W, par, i);
-		const int slot = P.slot;
-		// the slot's sums stay in registers while this thread owns the slot
-		float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
-		bool live = true;
-		while (live) {
-			Hit hh = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf)
-							: closest_hit(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err);
-			++segments;
-			live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
-				cm, q);
+	if constexpr (LINEAR) {
+		// every lane of a warp stays in the loop while any of its lanes has a path, so the
+		// warp-cooperative closest hit always runs with the full warp
+		WarpHitScratch &ws = scratch[threadIdx.x >> 5];
+		for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+			const unsigned i = base + threadIdx.x;
+			bool live = i < n;
+			PathState P{};
+			float4 sm{}, cm{}, q{};
+			if (live) {
+				P = load_path(W, par, i);
+				sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
+			}
+			const int slot = P.slot;
+			while (__any_sync(0xffffffffu, live)) {
+				Hit hh = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf, live, ws);
+				if (live) {
+					++segments;
+					live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done,
+						sm, cm, q);
+				}
+			}
+			if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 		}
-		W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
+	} else {
+		for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+			PathState P = load_path(W, par, i);
+			const int slot = P.slot;
+			// the slot's sums stay in registers while this thread owns the slot
+			float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
+			bool live = true;
+			while (live) {
+				Hit hh = closest_hit(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err);
+				++segments;
+				live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
+					cm, q);
+			}
+			W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
+		}
 	}
 	for (int o = 16; o > 0; o >>= 1) {
 		done += __shfl_down_sync(0xffffffffu, done, o);
@@ -321,6 +373,17 @@ int tail_grid(bool linear, int n_sms) {
 	return grid_for(linear ? (const void *)k_tail<true> : (const void *)k_tail<false>, n_sms);
 }
 
+void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par) {
+	if (linear)
+		k_intersect<true><<<grid, BLOCK, 0, s>>>(S, W, par);
+	else
+		k_intersect<false><<<grid, BLOCK, 0, s>>>(S, W, par);
+}
+
+int intersect_grid(bool linear, int n_sms) {
+	return grid_for(linear ? (const void *)k_intersect<true> : (const void *)k_intersect<false>, n_sms);
+}
+
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *prm, float *rgb, float *var,
 	are_render_stats *stats) {
 	if (!sc || !cam || !prm || !rgb) return bad("null scene, camera, params or output");
@@ -338,9 +401,9 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	// measured on GB300, the megakernel is the faster schedule on every workload scene (the path
 	// state stays in registers; no queue records go through memory between bounces)
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
-	const int g_int = grid_for((const void *)k_intersect, sc->n_sms);
-	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
 	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const int g_int = intersect_grid(linear, sc->n_sms);
+	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
 	const int g_tail = tail_grid(linear, sc->n_sms);
 
 	Wave W{};
@@ -460,7 +523,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 			int par = it & 1;
 			// external event nodes: the events are recorded each time the graph runs
 			cudaEventRecordWithFlags(kev[4 * it + 0], s, cudaEventRecordExternal);
-			k_intersect<<<g_int, BLOCK, 0, s>>>(S, W, par);
+			launch_intersect(linear, g_int, s, S, W, par);
 			cudaEventRecordWithFlags(kev[4 * it + 1], s, cudaEventRecordExternal);
 			k_shade<<<g_sh, BLOCK, 0, s>>>(S, W, par);
 			cudaEventRecordWithFlags(kev[4 * it + 2], s, cudaEventRecordExternal);
@@ -584,10 +647,15 @@ are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, i
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
 	if (!st) {
-		int grid = grid_for((const void *)k_intersect_batch, sc->n_sms);
+		const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+		int grid = grid_for(linear ? (const void *)k_intersect_batch<true> : (const void *)k_intersect_batch<false>,
+			sc->n_sms);
 		grid = (int)std::min<int64_t>(grid, (n + BLOCK - 1) / BLOCK);
 		cudaEventRecord(e0, s);
-		k_intersect_batch<<<grid, BLOCK, 0, s>>>(sc->dev, d_rays, n, d_hits, err_word);
+		if (linear)
+			k_intersect_batch<true><<<grid, BLOCK, 0, s>>>(sc->dev, d_rays, n, d_hits, err_word);
+		else
+			k_intersect_batch<false><<<grid, BLOCK, 0, s>>>(sc->dev, d_rays, n, d_hits, err_word);
 		cudaEventRecord(e1, s);
 		st = cuda_status(cudaGetLastError(), "k_intersect_batch launch");
 	}

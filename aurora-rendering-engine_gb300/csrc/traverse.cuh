@@ -101,14 +101,17 @@ __device__ __forceinline__ bool hit_quad(f3 Q, f3 u, f3 v, f3 o, f3 d, float tmi
 // Quad with the normal n = u x v and nn = n.n precomputed by the same rounded
 // operations as hit_quad, so the result is bit-identical to hit_quad's.
 //
-// Two early rejections skip the divisions without changing any answer:
-//  * with tmin >= 0, t = num/denom is <= 0 whenever num and denom differ in
-//    sign or num is 0, so such planes are behind the ray;
+// Two early rejections skip the divisions without changing any answer, both
+// for tmin >= 0 only (then every accepted t is positive):
+//  * t = num/denom is <= 0 whenever num and denom differ in sign or num is 0,
+//    so such planes are behind the ray;
 //  * with lim = tcut * |denom| * (1 + 2^-19) a normal float, |num| > lim means
-//    the correctly rounded quotient exceeds tcut (the best hit so far), so the
-//    quad cannot win; ties (t == tcut) are never rejected.
+//    the correctly rounded (positive) quotient exceeds tcut (the best hit so
+//    far), so the quad cannot win; ties (t == tcut) are never rejected.
+// With tmin < 0 a hit may lie behind the origin and every plane is divided.
 __device__ __forceinline__ bool quad_t_reject(float num, float denom, float tmin, float tcut) {
-	if (tmin >= 0.0f && !((num > 0.0f) == (denom > 0.0f) && num != 0.0f)) return true;
+	if (!(tmin >= 0.0f)) return false;
+	if (!((num > 0.0f) == (denom > 0.0f) && num != 0.0f)) return true;
 	float lim = tcut * fabsf(denom) * 1.000002f;
 	return lim >= 1.17549435e-38f && fabsf(num) > lim;
 }
@@ -315,6 +318,149 @@ __device__ __forceinline__ Hit closest_hit_linear(const float4 *__restrict__ sp,
 		best.u = __fdiv_rn(best.u, best_nn);
 		best.v = __fdiv_rn(best.v, best_nn);
 	}
+	return best;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-cooperative linear scan.  In closest_hit_linear every lane tests every
+// primitive whose leaf box it enters, so a warp issues the union of its
+// lanes' tests with a third of the lanes busy.  Here the warp first finds, for
+// all lanes together and one primitive at a time, the (ray, primitive) pairs
+// that can hit — the leaf box and, for quads, the side of the plane the ray
+// moves toward: exactly closest_hit_linear's own first rejections — and
+// queues them in a shared-memory ring; full rounds of 32 pairs then run the
+// complete tests with every lane busy, each lane on another lane's ray.  A
+// ray's best hit is the minimum of the 64-bit key (t bits << 32 | global id):
+// t is finite and > tmin >= 0 for every accepted hit, so the key orders like
+// closest_hit_linear's (t, global id) rule and the answer is the same bits.
+
+struct WarpHitScratch {
+	unsigned long long key[32];  // per lane: best (t bits << 32 | global id) so far; ~0 = none
+	float4 rec[32];              // per lane: u, v (quad: numerators), quad |n|^2 (else 0), leaf index
+	unsigned short ring[64];     // queued pairs (lane << 8 | leaf-order primitive)
+};
+
+__device__ __forceinline__ float key_t(unsigned long long k) {
+	return k == ~0ull ? __int_as_float(0x7f800000) : __uint_as_float((unsigned)(k >> 32));
+}
+
+// The test of staged primitive j, as in closest_hit_linear's inner loop; quads
+// report u, v as numerators over qnn.
+__device__ __forceinline__ bool test_staged(const float4 *__restrict__ sp, int j, int tri_wt, f3 o, f3 d, float tmin,
+	float tmax, float tcut, float &t, float &u, float &v, float &qnn, int &gid) {
+	const float4 p0 = sp[4 * j], p1 = sp[4 * j + 1];
+	gid = __float_as_int(p1.w);
+	u = v = qnn = 0.0f;
+	if (p0.w > 0.0f) return hit_sphere(p0, o, d, tmin, tmax, t);
+	const float4 p2 = sp[4 * j + 2];
+	if (p0.w == PRIM_TAG_QUAD) {
+		const float4 p3 = sp[4 * j + 3];
+		qnn = p3.w;
+		return hit_quad_pre(ld3(p0), ld3(p1), ld3(p2), ld3(p3), p3.w, o, d, tmin, tmax, tcut, t, u, v);
+	}
+	if (tri_wt) return hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+	return hit_tri_mt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+}
+
+// One round: lane k < n takes queued pair head + k and tests it on its
+// owner's ray and interval (shuffled in), then the owner's key keeps the
+// minimum and the pair that holds it records u, v.
+__device__ __forceinline__ void warp_hit_round(const float4 *__restrict__ sp, int tri_wt, f3 o, f3 d, float tmin,
+	float tmax, WarpHitScratch &ws, unsigned head, unsigned n) {
+	const unsigned lane = threadIdx.x & 31u;
+	const bool has = lane < n;
+	const unsigned e = has ? (unsigned)ws.ring[(head + lane) & 63u] : 0u;
+	const int owner = (int)(e >> 8), j = (int)(e & 0xffu);
+	const f3 oo{ __shfl_sync(0xffffffffu, o.x, owner), __shfl_sync(0xffffffffu, o.y, owner),
+		__shfl_sync(0xffffffffu, o.z, owner) };
+	const f3 dd{ __shfl_sync(0xffffffffu, d.x, owner), __shfl_sync(0xffffffffu, d.y, owner),
+		__shfl_sync(0xffffffffu, d.z, owner) };
+	const float t0 = __shfl_sync(0xffffffffu, tmin, owner), t1 = __shfl_sync(0xffffffffu, tmax, owner);
+	bool h = false;
+	float t = 0.0f, u = 0.0f, v = 0.0f, qnn = 0.0f;
+	unsigned long long k = ~0ull;
+	if (has) {
+		int gid;
+		h = test_staged(sp, j, tri_wt, oo, dd, t0, t1, key_t(ws.key[owner]), t, u, v, qnn, gid);
+		if (h) {
+			k = ((unsigned long long)__float_as_uint(t) << 32) | (unsigned)gid;
+			atomicMin(&ws.key[owner], k);
+		}
+	}
+	__syncwarp();
+	if (h && ws.key[owner] == k) ws.rec[owner] = make_float4(u, v, qnn, __int_as_float(j));
+	__syncwarp();
+}
+
+// Same answer as closest_hit_linear (per-lane rays and intervals) for rays
+// with tmin >= 0 (every hit then has t > 0, whose bits order like its value).
+// Every lane of the warp calls it at the same time (converged, full mask); a
+// lane with active == false adds no ray and gets a miss.
+__device__ __forceinline__ Hit closest_hit_linear_warp(const float4 *__restrict__ sp, int n_leaves, int tri_wt, f3 o,
+	f3 d, float tmin, float tmax, bool active, WarpHitScratch &ws) {
+	const unsigned lane = threadIdx.x & 31u;
+	const unsigned below = (1u << lane) - 1u;
+	ws.key[lane] = ~0ull;
+	float dx = d.x != 0.0f ? d.x : copysignf(1e-20f, d.x);
+	float dy = d.y != 0.0f ? d.y : copysignf(1e-20f, d.y);
+	float dz = d.z != 0.0f ? d.z : copysignf(1e-20f, d.z);
+	float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
+	float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+	unsigned queued = 0, head = 0;  // warp-uniform
+	__syncwarp();
+	for (int l = 0; l < n_leaves; ++l) {
+		// the leaf's padded box against this lane's best so far (culling only)
+		const float4 b0 = sp[4 * LINEAR_MAX + 2 * l], b1 = sp[4 * LINEAR_MAX + 2 * l + 1];
+		float t0x = fmaf(b0.x, ix, ox), t1x = fmaf(b1.x, ix, ox);
+		float t0y = fmaf(b0.y, iy, oy), t1y = fmaf(b1.y, iy, oy);
+		float t0z = fmaf(b0.z, iz, oz), t1z = fmaf(b1.z, iz, oz);
+		float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+		float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)),
+			fminf(fmaxf(t0z, t1z), fminf(key_t(ws.key[lane]), tmax) * 1.0000039f));
+		const bool pass = active && lo <= hi;
+		if (!__any_sync(0xffffffffu, pass)) continue;
+		const int first = __float_as_int(b0.w), end = first + __float_as_int(b1.w);
+		for (int j = first; j < end; ++j) {
+			const float4 p0 = sp[4 * j];
+			bool cand = pass;
+			if (p0.w == PRIM_TAG_QUAD) {
+				// hit_quad_pre's first rejections: plane parallel to the ray or behind it
+				const float4 p3 = sp[4 * j + 3];
+				const f3 n = ld3(p3);
+				const float denom = rdot(n, d);
+				const float num = rdot(n, rsub(ld3(p0), o));
+				cand = cand && denom != 0.0f && !(tmin >= 0.0f && !((num > 0.0f) == (denom > 0.0f) && num != 0.0f));
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, cand);
+			if (cand) ws.ring[(queued + (unsigned)__popc(m & below)) & 63u] = (unsigned short)((lane << 8) | (unsigned)j);
+			queued += (unsigned)__popc(m);
+			if (queued - head >= 32u) {
+				__syncwarp();
+				warp_hit_round(sp, tri_wt, o, d, tmin, tmax, ws, head, 32u);
+				head += 32u;
+			}
+		}
+	}
+	if (queued > head) {
+		__syncwarp();
+		warp_hit_round(sp, tri_wt, o, d, tmin, tmax, ws, head, queued - head);
+	}
+	__syncwarp();
+	Hit best;
+	best.t = __int_as_float(0x7f800000);
+	best.leaf = -1;
+	best.gid = 0x7fffffff;
+	best.u = best.v = 0.0f;
+	const unsigned long long k = ws.key[lane];
+	if (k != ~0ull) {
+		const float4 r = ws.rec[lane];
+		best.t = key_t(k);
+		best.gid = (int32_t)(unsigned)(k & 0xffffffffull);
+		best.leaf = __float_as_int(r.w);
+		best.u = r.z != 0.0f ? __fdiv_rn(r.x, r.z) : r.x;
+		best.v = r.z != 0.0f ? __fdiv_rn(r.y, r.z) : r.y;
+	}
+	__syncwarp();  // the scratch is free for the next call
 	return best;
 }
 

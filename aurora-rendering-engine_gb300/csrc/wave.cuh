@@ -48,12 +48,14 @@ constexpr size_t WAVE_SLOT_BYTES = 2 * 4 * sizeof(float4) + sizeof(float4) + 3 *
 void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f);
 
 __global__ void k_init(Wave W, int n_first);
-__global__ void k_intersect(DevScene S, Wave W, int par);
 __global__ void k_shade(DevScene S, Wave W, int par);
 __global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ var, int clamp);
 // k_tail (render.cu) for a scene scanned linearly (linear) or through its BVH, on queue 0;
 // tail_grid: its persistent grid (resident blocks x SMs)
 void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W);
 int tail_grid(bool linear, int n_sms);
+// k_intersect (render.cu) for a linear-scan or BVH scene on queue par, and its grid
+void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par);
+int intersect_grid(bool linear, int n_sms);
 
 }  // namespace are_core

@@ -127,6 +127,19 @@ def test_ray_extent_and_empty_scene(gpu_lib, oracle):
     assert np.all(hit_ids(h) == -1) and np.all(np.isinf(h[:, 0]))
 
 
+def test_negative_t_min_rays(gpu_lib, oracle):
+    """Rays whose interval starts behind the origin: warps holding such a ray
+    take the per-lane scan (hits at t <= 0 and ties between +0 and -0 keep the
+    (t, global id) order); the others the warp-cooperative one.  Both equal the
+    oracle bit for bit."""
+    s, _, _ = are.build_config(are.CONFIG_CORNELL)
+    r = random_rays(50_000, 17, lo=0, hi=555, t_min=1e-3, t_max=np.inf, frac_camera=0.0)  # origins in the room
+    r[: len(r) // 2 : 97, 3] = -300.0  # sparse in the first half, none in the second
+    h, _ = are.Scene(s).intersect(r)
+    assert_bitexact(oracle.intersect(oracle.prepare(s, accel=0), r), h, "negative t_min")
+    assert (h[: len(r) // 2 : 97, 0] < 0).any()  # some hits behind the origin were found
+
+
 def test_device_pointer_path(gpu_lib, oracle):
     torch = pytest.importorskip("torch")
     s, _, _ = are.build_config(are.CONFIG_RANDOM_SPHERES)
