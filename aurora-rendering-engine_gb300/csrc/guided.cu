@@ -49,8 +49,10 @@ struct GuidedState {
 // list: every diffuse hit at depth < guide_depth gets its features written to
 // the compact list (its row in gidx), so inference runs on that list only.
 // The compact list's counter W.cnt[6] is zeroed before this kernel.
+template <bool LINEAR>
 __global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, GuidedState G, int par) {
-	__shared__ float4 snodes[2 * SMEM_NODES];
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -58,8 +60,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, 
 		atomicAdd(&W.stat[0], (unsigned long long)n);
 	}
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
-	const bool linear = S.n_prims <= LINEAR_MAX;
-	if (linear) {
+	if (LINEAR) {
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else {
@@ -71,11 +72,16 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, 
 		const unsigned i = base + threadIdx.x;
 		bool sel = false;
 		float x[GN_IN];
+		float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+		if (i < n) a = W.qa[par][i], b = W.qb[par][i];
+		Hit h;
+		if (LINEAR)  // warp-cooperative: every lane of the warp takes part
+			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(a), ld3(b), W.t_min, inf, i < n,
+				scratch[threadIdx.x >> 5]);
+		else if (i < n)
+			h = closest_hit(S, snodes, n_snodes, ld3(a), ld3(b), W.t_min, inf, err);
 		if (i < n) {
-			const float4 a = W.qa[par][i], b = W.qb[par][i];
 			const f3 o = ld3(a), d = ld3(b);
-			const Hit h = linear ? closest_hit_linear(snodes, S.n_leaves, S.triangle_test, o, d, W.t_min, inf)
-								 : closest_hit(S, snodes, n_snodes, o, d, W.t_min, inf, err);
 			W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 			const int depth = __float_as_int(b.w) & 0xff;
 			if (h.leaf >= 0 && depth < G.guide_depth) {
@@ -360,6 +366,11 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	cudaEvent_t ev0, ev1;
 	cudaEventCreate(&ev0);
 	cudaEventCreate(&ev1);
+	// per graph iteration: before intersect, after intersect, after inference, after shade;
+	// then two around each batch of training steps
+	cudaEvent_t kev[4 * GUIDED_ITERS + 2];
+	for (auto &e : kev) cudaEventCreate(&e);
+	double kms[4] = { 0.0, 0.0, 0.0, 0.0 };
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	int64_t iterations = 0, train_steps = 0;
@@ -375,7 +386,9 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_init");
 	}
-	const int g_int = grid_of((const void *)k_intersect_select, sc->n_sms);
+	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const void *isect_fn = linear ? (const void *)k_intersect_select<true> : (const void *)k_intersect_select<false>;
+	const int g_int = grid_of(isect_fn, sc->n_sms);
 	const int g_sh = grid_of((const void *)k_shade_guided, sc->n_sms);
 	const DevScene S = sc->dev;
 	// the network runs on the compact list, its length read on the device
@@ -384,16 +397,23 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		for (int it = 0; it < GUIDED_ITERS; ++it) {
 			int par = it & 1;
 			cudaMemsetAsync(W.cnt + 6, 0, 4, s);
-			k_intersect_select<<<g_int, BLOCK, 0, s>>>(S, W, G, par);
+			cudaEventRecordWithFlags(kev[4 * it + 0], s, cudaEventRecordExternal);
+			if (linear)
+				k_intersect_select<true><<<g_int, BLOCK, 0, s>>>(S, W, G, par);
+			else
+				k_intersect_select<false><<<g_int, BLOCK, 0, s>>>(S, W, G, par);
+			cudaEventRecordWithFlags(kev[4 * it + 1], s, cudaEventRecordExternal);
 			net->infer(G.gfeat, P, G.gout, s, W.cnt + 6, W.cnt + 4, true);
+			cudaEventRecordWithFlags(kev[4 * it + 2], s, cudaEventRecordExternal);
 			k_shade_guided<<<g_sh, BLOCK, 0, s>>>(S, W, G, par);
+			cudaEventRecordWithFlags(kev[4 * it + 3], s, cudaEventRecordExternal);
 		}
 		st = cuda_status(cudaStreamEndCapture(s, &graph), "capture end");
 	}
 	if (!st) st = cuda_status(cudaGraphInstantiate(&exec, graph, 0), "instantiate");
 	const int64_t max_launches = (int64_t)(W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk + 16;
 	unsigned *hc = sc->host_counters;
-	bool pending_loss = false;
+	bool pending_loss = false, pending_train = false;
 	unsigned pending_n = 1;
 	// a step needs a quarter batch: fewer samples make a noisy gradient
 	const unsigned tmin = std::max(256u, tcap / 4);
@@ -405,7 +425,21 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		if (st) break;
 		iterations += GUIDED_ITERS;
 		launches[ARE_KERNEL_INTERSECT] += GUIDED_ITERS;
-		launches[ARE_KERNEL_SHADE] += 2 * GUIDED_ITERS;  // inference, shade (+ training samples, accumulate, generate)
+		launches[ARE_KERNEL_GENERATE] += GUIDED_ITERS;  // inference
+		launches[ARE_KERNEL_SHADE] += GUIDED_ITERS;     // shade (+ training samples, accumulate, next camera ray)
+		for (int it = 0; it < GUIDED_ITERS; ++it) {
+			static const int kind[3] = { ARE_KERNEL_INTERSECT, ARE_KERNEL_GENERATE, ARE_KERNEL_SHADE };
+			for (int k = 0; k < 3; ++k) {
+				float ms = 0.f;
+				if (cudaEventElapsedTime(&ms, kev[4 * it + k], kev[4 * it + k + 1]) == cudaSuccess) kms[kind[k]] += ms;
+			}
+		}
+		if (pending_train) {
+			float ms = 0.f;
+			if (cudaEventElapsedTime(&ms, kev[4 * GUIDED_ITERS], kev[4 * GUIDED_ITERS + 1]) == cudaSuccess)
+				kms[ARE_KERNEL_OTHER] += ms;
+			pending_train = false;
+		}
 		const unsigned have = std::min(hc[7], tcap);
 		if (pending_loss) {
 			// the loss of the step enqueued after the previous launch is complete now
@@ -415,11 +449,14 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		if (gp->train && have >= tmin) {
 			// `train` Adam steps on what was collected (up to one batch), then collect again
 			net->weight_clip = gp->weight_clip > 0.f ? gp->weight_clip : 1e30f;
+			cudaEventRecord(kev[4 * GUIDED_ITERS], s);
 			for (int k = 0; k < gp->train && !st; ++k) {
 				st = net->train_step(G.tbuf, (int)have, -1.0f, gp->lr, s);
 				++train_steps;
 				launches[ARE_KERNEL_OTHER] += 7;
 			}
+			cudaEventRecord(kev[4 * GUIDED_ITERS + 1], s);
+			pending_train = true;  // timed once the next launch's read-back has synchronised
 			cudaMemcpyAsync(hc + 16, net->grad + GN_PARAMS, 4, cudaMemcpyDeviceToHost, s);
 			pending_loss = true;
 			pending_n = have;
@@ -456,6 +493,12 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	if (graph) cudaGraphDestroy(graph);
 	cudaEventDestroy(ev0);
 	cudaEventDestroy(ev1);
+	if (!st && pending_train) {
+		float tms = 0.f;
+		if (cudaEventElapsedTime(&tms, kev[4 * GUIDED_ITERS], kev[4 * GUIDED_ITERS + 1]) == cudaSuccess)
+			kms[ARE_KERNEL_OTHER] += tms;
+	}
+	for (auto &e : kev) cudaEventDestroy(e);
 	cudaStreamSynchronize(s);
 	cudaFree(mem);
 	if (!st && herr) {
@@ -468,7 +511,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		stats->segments = (int64_t)hstat[0];
 		stats->iterations = iterations;
 		stats->device_ms = ms;
-		for (int k = 0; k < 4; ++k) stats->kernel_launches[k] = launches[k];
+		for (int k = 0; k < 4; ++k) stats->kernel_launches[k] = launches[k], stats->kernel_ms[k] = kms[k];
 		stats->error_word = (int32_t)herr;
 		stats->aux[0] = (double)hstat[2];
 		stats->aux[1] = (double)train_steps;

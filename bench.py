@@ -61,6 +61,9 @@ BYTES_SHADE_SAMPLE = 48 + 48       # per sample: the slot's Kahan accumulators r
 # megakernel keeps all of it on chip, so its DRAM traffic is far below these
 BYTES_MEGA_SAMPLE = 152
 BYTES_MEGA_SEGMENT = 260
+GUIDE_FLOPS_PER_ROW = 2 * (256 * 64 + 3 * 64 * 64 + 64 * 48)  # the network's multiply-adds, padded shapes
+GUIDE_BYTES_IN = 36                 # per network row: 9 FP32 features written by intersect_select
+GUIDE_BYTES_MIXTURE = 192           # per network row: the packed 8-lobe mixture read by shading
 
 
 def dist_env():
@@ -141,8 +144,9 @@ def measured_peaks() -> dict:
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops", 1900.0),
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", 1700.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
 def cpu_sample(scene, cam, par, budget_s: float, threads: int) -> dict:
@@ -365,6 +369,33 @@ def run_guided(args, rank, world) -> None:
     barrier(world)
     dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
     samples = W * H * spp
+    # per kernel: intersect (+ network input list), inference, guided shading, training
+    tot = {k: sum(s["kernel_ms"][k] for s in stats) for k in are.KERNELS}
+    launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
+    segs = sum(s["segments"] for s in stats)
+    rows = sum(s["guided_vertices"] for s in stats)
+    smp = samples * len(stats)
+    peaks = measured_peaks()
+    dom = max(("intersect", "generate", "shade"), key=lambda k: tot[k])
+    if dom == "generate":  # the network on the tensor cores: its own FLOPs
+        flops = rows * GUIDE_FLOPS_PER_ROW
+        ach = flops / (tot[dom] / 1e3) / 1e12
+        roof = {"kernel": "k_guide_infer", "bound": "tensor", "achieved": round(ach, 1),
+                "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                "frac": round(ach / peaks["bf16_tflops_sustained"], 4), "peak_source": peaks["source"] + " (sustained)",
+                "flops_per_launch": round(flops / max(1, launches[dom]))}
+    else:
+        algo = {"intersect": BYTES_INTERSECT * segs + GUIDE_BYTES_IN * rows,
+                "shade": BYTES_SHADE_SEGMENT * segs + GUIDE_BYTES_MIXTURE * rows + BYTES_SHADE_SAMPLE * smp}[dom]
+        ach = algo / (tot[dom] / 1e3) / 1e9
+        roof = {"kernel": {"intersect": "k_intersect_select", "shade": "k_shade_guided"}[dom], "bound": "hbm",
+                "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
+                "bytes_per_launch": round(algo / max(1, launches[dom]))}
+    roof.update({"avg_launch_us": round(tot[dom] * 1e3 / max(1, launches[dom]), 2),
+                 "kernel_ms": {"intersect_select": round(tot["intersect"], 2), "inference": round(tot["generate"], 2),
+                               "shade": round(tot["shade"], 2), "training": round(tot["other"], 2)},
+                 "traffic": None})
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(world * samples * args.steps / (dev_ms / 1e3) / 1e6, 3), "unit": UNIT,
@@ -377,6 +408,7 @@ def run_guided(args, rank, world) -> None:
             "adam_steps_per_frame": round(sum(s["train_steps"] for s in stats) / len(stats), 1),
             "guided_vertices_per_sample": round(sum(s["guided_vertices"] for s in stats) / (samples * len(stats)), 3),
             "segments_per_sample": round(sum(s["segments"] for s in stats) / (samples * len(stats)), 4),
+            "roofline": roof,
             "clocks": clk.summary(),
             "gpu_launches": sum(sum(s["kernel_launches"].values()) for s in stats),
         }

@@ -304,7 +304,11 @@ typedef struct are_guide_params {
  * weighted by the combined density, so the image stays unbiased whatever the
  * network has learned.  With train != 0 the network trains on the render's
  * own paths; stats->aux holds the training samples emitted, the Adam steps
- * taken, the guided vertices and the last loss. */
+ * taken, the guided vertices and the last loss.  It always runs the wavefront
+ * (the network sees each bounce's rows as one batch); stats->kernel_ms holds
+ * [ARE_KERNEL_INTERSECT] closest hits and input selection, [ARE_KERNEL_GENERATE]
+ * network inference, [ARE_KERNEL_SHADE] guided shading, [ARE_KERNEL_OTHER]
+ * the training steps. */
 ARE_API are_status are_render_guided(are_scene *scene, are_guide *guide, const are_camera *camera,
 	const are_render_params *params, const are_guide_params *guide_params, float *rgb_out, float *var_out,
 	are_render_stats *stats);
