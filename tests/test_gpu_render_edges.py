@@ -1,0 +1,102 @@
+"""Edge cases of are_render on both schedules (megakernel, wavefront): an
+empty scene, a one-pixel frame, paths of a single segment, and scenes on
+either side of the linear-scan limit (48 primitives: the warp-cooperative
+scan of staged primitives; 49: the BVH).  Closest hits bit-exact against the
+oracle; images between the schedules bit for bit and against the oracle's
+same-seed render."""
+import numpy as np
+import pytest
+
+from common import are, hit_ids, random_rays
+
+pytestmark = pytest.mark.gpu
+
+SCHEDULES = (are.SCHEDULE_MEGAKERNEL, are.SCHEDULE_WAVEFRONT)
+LINEAR_MAX = 48  # core.h
+
+
+def render_both(sc, cam, par):
+    """Both schedules with the same chunk: the same image and statistics."""
+    out = [sc.render(cam, dict(par, schedule=s)) for s in SCHEDULES]
+    (a, va, sa), (b, vb, sb) = out
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["samples"] == sb["samples"] and sa["segments"] == sb["segments"]
+    assert sa["error_word"] == sb["error_word"] == 0
+    return a, va, sa
+
+
+def test_empty_scene_is_the_background(gpu_lib):
+    s = are.SceneArrays()
+    s.material()
+    s.bg_a = (0.25, 0.5, 0.75)
+    cam = dict(lookfrom=(0, 0, 0), lookat=(0, 0, -1), vup=(0, 1, 0), vfov_deg=60.0, aperture=0.0, focus_dist=1.0)
+    par = dict(width=17, height=9, spp=8, max_depth=8, seed=3, rr_depth=3, t_min=1e-3, chunk=2)
+    img, var, st = render_both(are.Scene(s), cam, par)
+    assert st["samples"] == 17 * 9 * 8 and st["segments"] == st["samples"]  # one miss per path
+    assert np.allclose(img, np.asarray(s.bg_a, np.float32), rtol=1e-6, atol=0)
+    assert np.all(var <= 1e-12)
+
+
+def test_one_pixel_frame(gpu_lib, oracle, nthreads):
+    s, cam, par = are.build_config(are.CONFIG_CORNELL)
+    par = dict(par, width=1, height=1, spp=256, chunk=16)
+    img, var, st = render_both(are.Scene(s), cam, par)
+    m, v, st_cpu = oracle.render(oracle.prepare(s), cam, par, nthreads=nthreads)
+    assert st["samples"] == st_cpu["samples"] == 256
+    assert np.all(np.abs(img - m) <= 5 * np.sqrt(var + v) + 1e-6)
+
+
+def test_single_segment_paths(gpu_lib, oracle, nthreads):
+    """max_depth 1: a path is its camera ray; the image is the emission seen
+    directly, the same rays and hits as the oracle's."""
+    s, cam, par = are.build_config(are.CONFIG_CORNELL)
+    par = dict(par, width=40, height=40, spp=16, max_depth=1, chunk=4)
+    img, var, st = render_both(are.Scene(s), cam, par)
+    m, v, st_cpu = oracle.render(oracle.prepare(s), cam, par, nthreads=nthreads)
+    assert st["segments"] == st["samples"] == st_cpu["samples"] == 40 * 40 * 16
+    assert img.max() > 0  # the light is in view
+    assert np.allclose(img, m, rtol=1e-5, atol=1e-6)
+
+
+def random_scene(n: int, seed: int) -> are.SceneArrays:
+    """n primitives in a unit box around the origin (quads, spheres and
+    watertight triangles in turn), a white diffuse material and a light."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = are.SceneArrays()
+    white = s.material(albedo=(0.7, 0.7, 0.7))
+    lamp = s.material(are.MAT_DIFFUSE_LIGHT, emit=(4.0, 4.0, 4.0))
+    s.background = are.BG_SKY_GRADIENT
+    s.bg_a, s.bg_b = (1.0, 1.0, 1.0), (0.5, 0.7, 1.0)
+    for k in range(n):
+        c = rng.uniform(-1, 1, 3)
+        mat = lamp if k % 11 == 0 else white
+        if k % 3 == 0:
+            s.add_quads(np.concatenate([c, rng.normal(size=3) * 0.3, rng.normal(size=3) * 0.3]), mat)
+        elif k % 3 == 1:
+            s.add_spheres([*c, rng.uniform(0.05, 0.2)], mat)
+        else:
+            s.add_triangles(np.concatenate([c, c + rng.normal(size=3) * 0.3, c + rng.normal(size=3) * 0.3]), mat)
+    return s
+
+
+@pytest.mark.parametrize("n", [LINEAR_MAX, LINEAR_MAX + 1])
+def test_linear_scan_limit(gpu_lib, oracle, nthreads, n):
+    s = random_scene(n, 40 + n)
+    assert s.n_prims == n
+    sc = are.Scene(s)
+    r = random_rays(200_000, n, lo=-1.5, hi=1.5, t_min=1e-4, t_max=np.inf, camera=(0, 0, 4))
+    h, _ = sc.intersect(r)
+    ref = oracle.intersect(oracle.prepare(s, accel=0), r, nthreads)
+    ih, ir = hit_ids(h), hit_ids(ref)
+    assert np.array_equal(ih, ir)
+    m = ih >= 0
+    assert m.mean() > 0.03  # ~15k hits of 200k rays among small primitives
+    assert np.array_equal(h[m][:, [0, 2, 3]].view(np.uint32), ref[m][:, [0, 2, 3]].view(np.uint32))
+    cam = dict(lookfrom=(0, 0, 4), lookat=(0, 0, 0), vup=(0, 1, 0), vfov_deg=45.0, aperture=0.0, focus_dist=4.0)
+    par = dict(width=48, height=32, spp=32, max_depth=8, seed=5, rr_depth=3, t_min=1e-4, chunk=8)
+    img, var, st = render_both(sc, cam, par)
+    mc, vc, _ = oracle.render(oracle.prepare(s), cam, par, nthreads=nthreads)
+    sd = np.sqrt(var + vc)
+    out = (sd > 0) & (np.abs(img - mc) > 4 * sd)
+    assert out.mean() < 0.01, out.mean()
