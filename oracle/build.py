@@ -20,6 +20,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
+# where the reference tree lies in the development container (absent on GPU hosts)
+REF_ROOT = Path(os.environ.get("ARE_REFERENCE_ROOT", "/root/reference"))
 ORACLE_SOURCES = ["orc_common.c", "orc_f32.c", "orc_f64.c", "orc_legacy.c", "orc_guide.c"]
 REF_LIB_SOURCES = [
     "src/basic/vec3.cpp",
@@ -59,7 +61,7 @@ def build_oracle(force: bool = False) -> Path:
     return out
 
 
-def build_ref(ref_root: str | os.PathLike = "/root/reference", force: bool = False) -> list[Path]:
+def build_ref(ref_root: str | os.PathLike = REF_ROOT, force: bool = False) -> list[Path]:
     """Compile the reference's sources into oracle/_ref (returns the .so paths)."""
     root = Path(ref_root)
     if not (root / "experiments" / "rt.cpp").exists():
