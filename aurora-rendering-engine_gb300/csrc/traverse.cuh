@@ -466,8 +466,12 @@ __device__ __forceinline__ Hit closest_hit_linear_warp(const float4 *__restrict_
 
 // Closest hit with the (t, global id) order.  `snodes` holds the first
 // `n_snodes` nodes in shared memory.  err receives ERR_* bits.
+// SHORT > 0: the first SHORT stack entries live in shared memory, `sstack`
+// holding this thread's column (entry k at sstack[k * blockDim.x]), the rest
+// in local memory; SHORT == 0: the whole stack in local memory.
+template <int SHORT = 0>
 __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
-	f3 d, float tmin, float tmax, uint32_t &err) {
+	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack = nullptr) {
 	Hit best;
 	best.t = __int_as_float(0x7f800000);
 	best.leaf = -1;
@@ -483,8 +487,8 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 	const int32_t tri_wt = S.triangle_test;
 	if (S.n_prims == 0) return best;
 
-	int2 stack[MAX_STACK];
-	float stack_t[MAX_STACK];  // entry distance of each pushed node
+	int2 stack[MAX_STACK - SHORT];
+	float stack_t[MAX_STACK - SHORT];  // entry distance of each pushed node
 	int sp = 0;
 	// current node (a, b): start with the root's
 	float4 r1 = n_snodes > 0 ? snodes[1] : ldg4(G + 1);
@@ -542,9 +546,11 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 					nearn = farn;
 					farn = t;
 				}
-				if (sp < MAX_STACK) {
-					stack_t[sp] = fmaxf(l0, l1);
-					stack[sp++] = farn;
+				if (SHORT > 0 && sp < SHORT) {
+					sstack[sp++ * (int)blockDim.x] = make_int4(farn.x, farn.y, __float_as_int(fmaxf(l0, l1)), 0);
+				} else if (sp < MAX_STACK) {
+					stack_t[sp - SHORT] = fmaxf(l0, l1);
+					stack[sp++ - SHORT] = farn;
 				} else {
 					err |= ERR_STACK_OVERFLOW;
 				}
@@ -596,9 +602,19 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 		bool found = false;
 		while (sp > 0) {
 			--sp;
-			if (stack_t[sp] <= best.t * 1.0000039f) {
-				a = stack[sp].x;
-				b = stack[sp].y;
+			int2 e;
+			float te;
+			if (SHORT > 0 && sp < SHORT) {
+				const int4 r = sstack[sp * (int)blockDim.x];
+				e = make_int2(r.x, r.y);
+				te = __int_as_float(r.z);
+			} else {
+				e = stack[sp - SHORT];
+				te = stack_t[sp - SHORT];
+			}
+			if (te <= best.t * 1.0000039f) {
+				a = e.x;
+				b = e.y;
 				found = true;
 				break;
 			}
