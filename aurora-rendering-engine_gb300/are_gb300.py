@@ -75,6 +75,7 @@ class SceneArrays:
     triangle_test: int = TRI_WATERTIGHT
     bvh_leaf_size: int = 0
     bvh_build: int = 0
+    bvh_width: int = 0
 
     @property
     def n_prims(self) -> int:
@@ -138,7 +139,7 @@ class SceneDesc(C.Structure):
         ("n_texels", C.c_int64), ("texels", _f),
         ("background", C.c_int32), ("bg_a", C.c_float * 3), ("bg_b", C.c_float * 3),
         ("triangle_test", C.c_int32), ("bvh_leaf_size", C.c_int32), ("bvh_build", C.c_int32),
-    ]
+        ("bvh_width", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -254,6 +255,7 @@ def desc_struct(s: SceneArrays) -> tuple[SceneDesc, list]:
     d.triangle_test = int(s.triangle_test)
     d.bvh_leaf_size = int(s.bvh_leaf_size)
     d.bvh_build = int(s.bvh_build)
+    d.bvh_width = int(s.bvh_width)
     return d, keep
 
 
@@ -281,6 +283,7 @@ def arrays_from_desc(d: SceneDesc) -> SceneArrays:
     s.texels = _copy(d.texels, d.n_texels, 3) if d.n_texels else None
     s.background, s.bg_a, s.bg_b = d.background, tuple(d.bg_a), tuple(d.bg_b)
     s.triangle_test, s.bvh_leaf_size, s.bvh_build = d.triangle_test, d.bvh_leaf_size, d.bvh_build
+    s.bvh_width = d.bvh_width
     return s
 
 

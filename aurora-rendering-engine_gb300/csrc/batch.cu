@@ -55,6 +55,9 @@ __device__ __forceinline__ unsigned long long gtimer() {
 	return t;
 }
 
+// ANY_WIDE: some scene of the batch has a 4-wide tree (each query then picks its scene's tree);
+// otherwise every query walks the binary tree
+template <bool ANY_WIDE>
 __global__ void k_batch(const BatchScene *__restrict__ T, int n_scenes, BatchCtl C, int fetch) {
 	if (threadIdx.x == 0) atomicMin(C.start, gtimer());
 	const unsigned lane = threadIdx.x & 31u;
@@ -91,7 +94,8 @@ __global__ void k_batch(const BatchScene *__restrict__ T, int n_scenes, BatchCtl
 				f3 beta{ 1.f, 1.f, 1.f }, L{ 0.f, 0.f, 0.f };
 				for (int depth = 0; depth < B.max_depth; ++depth) {
 					++segs;
-					Hit h = closest_hit(B.S, nullptr, 0, o, d, B.t_min, inf, err);
+					Hit h = ANY_WIDE ? closest_hit_any(B.S, nullptr, 0, o, d, B.t_min, inf, err)
+									 : closest_hit(B.S, nullptr, 0, o, d, B.t_min, inf, err);
 					if (h.leaf < 0) {
 						L = add(L, mulv(beta, background(B.S, d)));
 						break;
@@ -238,13 +242,19 @@ are_status render_batch(are_scene *const *scenes, const are_camera *cams, const 
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	if (!st) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+	bool any_wide = false;
+	for (int i = 0; i < n; ++i) any_wide = any_wide || table[i].S.n_nodes4 > 0;
+	const void *batch_fn = any_wide ? (const void *)k_batch<true> : (const void *)k_batch<false>;
 	int per_sm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_batch, block, 0);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_fn, block, 0);
 	const int grid = std::max(1, per_sm) * n_sms;
 	if (!st) {
 		k_batch_init<<<(n + 255) / 256, 256, 0, s>>>(d_table, n, C);
 		cudaMemsetAsync(mem, 0, acc_bytes, s);
-		k_batch<<<grid, block, 0, s>>>(d_table, n, C, fetch);
+		if (any_wide)
+			k_batch<true><<<grid, block, 0, s>>>(d_table, n, C, fetch);
+		else
+			k_batch<false><<<grid, block, 0, s>>>(d_table, n, C, fetch);
 		for (int i = 0; i < n; ++i)
 			k_batch_resolve<<<std::max(1, std::min(1024, (table[i].npix + 255) / 256)), 256, 0, s>>>(table[i].acc,
 				table[i].npix, table[i].spp, d_out[i], nullptr);

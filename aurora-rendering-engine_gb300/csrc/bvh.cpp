@@ -377,4 +377,106 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 	return r;
 }
 
+std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes) {
+	std::vector<float> out;
+	const float *rec = bvh.nodes.data();
+	auto is_leaf = [&](int32_t r) {
+		int32_t b;
+		std::memcpy(&b, &rec[8 * (size_t)r + 7], 4);
+		return b != 0;
+	};
+	auto child = [&](int32_t r) {
+		int32_t a;
+		std::memcpy(&a, &rec[8 * (size_t)r + 3], 4);
+		return a;
+	};
+	auto area = [&](int32_t r) {
+		const float *o = &rec[8 * (size_t)r];
+		double dx = (double)o[4] - o[0], dy = (double)o[5] - o[1], dz = (double)o[6] - o[2];
+		return dx * dy + dy * dz + dz * dx;
+	};
+	if (bvh.n_nodes < 4 || is_leaf(0)) return out;
+	// children (binary record indices) of the wide node made from binary interior record r
+	auto gather = [&](int32_t r, int32_t kids[4]) {
+		int n = 2;
+		kids[0] = child(r), kids[1] = child(r) + 1;
+		while (n < 4) {
+			int best = -1;
+			double ba = -1.0;
+			for (int k = 0; k < n; ++k)
+				if (!is_leaf(kids[k]) && area(kids[k]) > ba) ba = area(kids[k]), best = k;
+			if (best < 0) break;
+			const int32_t c = child(kids[best]);
+			kids[best] = c;
+			kids[n++] = c + 1;
+		}
+		return n;
+	};
+	// wide nodes in order: breadth-first, then depth-first (as the binary layout)
+	std::vector<int32_t> src;  // binary interior record of each wide node
+	src.push_back(0);
+	std::deque<int32_t> work;  // wide node indices whose children are not numbered yet
+	work.push_back(0);
+	std::vector<std::array<int32_t, 4>> refs;  // per wide node: wide index of each interior child, -1 otherwise
+	std::vector<std::array<int32_t, 4>> kids_of;
+	std::vector<int> nkids;
+	refs.push_back({ -1, -1, -1, -1 });
+	kids_of.push_back({ -1, -1, -1, -1 });
+	nkids.push_back(0);
+	while (!work.empty()) {
+		int32_t w;
+		if ((int)src.size() < bfs_nodes) {
+			w = work.front();
+			work.pop_front();
+		} else {
+			w = work.back();
+			work.pop_back();
+		}
+		int32_t kids[4];
+		const int n = gather(src[w], kids);
+		nkids[w] = n;
+		std::vector<int32_t> inner;
+		for (int k = 0; k < n; ++k) {
+			kids_of[w][k] = kids[k];
+			if (is_leaf(kids[k])) continue;
+			const int32_t m = (int32_t)src.size();
+			src.push_back(kids[k]);
+			refs.push_back({ -1, -1, -1, -1 });
+			kids_of.push_back({ -1, -1, -1, -1 });
+			nkids.push_back(0);
+			refs[w][k] = m;
+			inner.push_back(m);
+		}
+		if ((int)src.size() < bfs_nodes) {
+			for (int32_t m : inner) work.push_back(m);
+		} else {  // depth-first: the first child next
+			for (auto it = inner.rbegin(); it != inner.rend(); ++it) work.push_back(*it);
+		}
+	}
+	const size_t nw = src.size();
+	out.assign(32 * nw, 0.0f);
+	for (size_t w = 0; w < nw; ++w) {
+		for (int k = 0; k < 4; ++k) {
+			float *o = &out[32 * w + 8 * (size_t)k];
+			if (k >= nkids[w]) {
+				// unused slot: an empty leaf (count -1, no primitives), so entering it does nothing
+				// (a min > max box is no guard: the slab test orders each axis's two planes)
+				const int32_t a = 0, b = -1;
+				for (int j = 0; j < 3; ++j) o[j] = 1.0f, o[4 + j] = -1.0f;
+				std::memcpy(&o[3], &a, 4);
+				std::memcpy(&o[7], &b, 4);
+				continue;
+			}
+			const int32_t r = kids_of[w][k];
+			std::memcpy(o, &rec[8 * (size_t)r], 32);  // box, first / count as in the binary record
+			if (!is_leaf(r)) {
+				const int32_t a = refs[w][k], b = 0;
+				std::memcpy(&o[3], &a, 4);
+				std::memcpy(&o[7], &b, 4);
+			}
+		}
+	}
+	return out;
+}
+
 }  // namespace are_core

@@ -29,4 +29,16 @@ struct BvhResult {
 // a box whose primitive a separate FP32 primitive test would hit.
 BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size);
 
+// The same tree with four children per node: every node of the result is four
+// 32-byte child records in the binary tree's record format (box, a; box, b:
+// b == 0 marks an interior child whose four records start at 4 a, b > 0 a leaf
+// of b primitives from a), 128 bytes; unused slots are empty leaves (b = -1).  A
+// node's children are the binary node's children, each interior one replaced
+// by its own two children, largest surface area first, until four (the usual
+// collapse of a binary SAH tree).  Nodes are numbered breadth-first for the
+// first `bfs_nodes` (the shared-memory top levels), depth-first after.  The
+// root's own box stays in the binary tree's record 0.  Empty when the binary
+// root is a leaf (the tree has fewer than two levels).
+std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes);
+
 }  // namespace are_core

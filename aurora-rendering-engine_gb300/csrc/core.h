@@ -28,6 +28,9 @@ constexpr float PRIM_TAG_TRI = -2.0f;
 constexpr int MAX_STACK = 64;      // traversal stack entries per ray
 constexpr int MAX_BVH_DEPTH = 60;  // the builder never exceeds this
 constexpr int SMEM_NODES = 1024;   // top BVH nodes staged in shared memory (32 KB)
+constexpr int SMEM_NODES4 = 256;   // the same 32 KB as 4-wide nodes (128 bytes each)
+constexpr int MAX_STACK4 = 96;     // 4-wide traversal: up to 3 entries per level
+constexpr int WIDE_BVH_MIN_PRIMS = 1 << 19;  // automatic bvh_width: 4-wide above this many primitives
 // scenes with at most this many primitives are scanned linearly from shared
 // memory (4 float4 per primitive) instead of traversing the BVH
 constexpr int LINEAR_MAX = 48;
@@ -40,6 +43,7 @@ enum : uint32_t {
 	ERR_BAD_INDEX = 4u,
 	ERR_NONFINITE = 8u,
 	ERR_TENSOR_TIMEOUT = 16u,  // a bounded wait for tensor-core work or a bulk copy gave up
+	ERR_BVH_WALK = 32u,        // a traversal visited more nodes than the tree has (malformed tree): stopped
 };
 
 struct DevMaterial {  // mirrors are_material (48 B)
@@ -65,6 +69,8 @@ struct DevScene {
 	const int32_t *prim_mat;
 	const float *tri_uv;       // null if the scene has no per-vertex uv
 	const float4 *nodes;
+	const float4 *nodes4;      // 4-wide tree (8 float4 per node), null if not built
+	int32_t n_nodes4;
 	const float4 *leaves;      // leaf boxes (node format) when n_prims <= LINEAR_MAX
 	int32_t n_leaves;
 	const DevMaterial *mats;

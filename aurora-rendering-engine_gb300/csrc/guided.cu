@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, 
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else {
-		stage_nodes(S, snodes, n_snodes);
+		stage_bvh(S, snodes, n_snodes);
 	}
 	uint32_t err = 0;
 	const float inf = __int_as_float(0x7f800000);
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_select(DevScene S, Wave W, 
 			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(a), ld3(b), W.t_min, inf, i < n,
 				scratch[threadIdx.x >> 5]);
 		else if (i < n)
-			h = closest_hit(S, snodes, n_snodes, ld3(a), ld3(b), W.t_min, inf, err);
+			h = closest_hit_any(S, snodes, n_snodes, ld3(a), ld3(b), W.t_min, inf, err);
 		if (i < n) {
 			const f3 o = ld3(a), d = ld3(b);
 			W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);

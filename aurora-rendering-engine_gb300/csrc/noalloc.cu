@@ -107,7 +107,7 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	if (cudaSetDevice(sc->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
 	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
-	const int g_tail = tail_grid(linear, sc->n_sms);
+	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
 	unsigned char *base = nullptr;
 	if (are_status st = scratch_address(sc->device, &base)) return st;
 

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else {
-		stage_nodes(S, snodes, n_snodes);
+		stage_bvh(S, snodes, n_snodes);
 	}
 	uint32_t err = 0;
 	// whole warps walk the rays together (the linear scan is warp-cooperative)
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect_batch(DevScene S, const flo
 		} else if (linear && active) {
 			h = closest_hit_linear(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), r0.w, r1.w);
 		} else if (active) {
-			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
+			h = closest_hit_any(S, snodes, n_snodes, ld3(r0), ld3(r1), r0.w, r1.w, err);
 		}
 		if (active)
 			hits[i] = h.leaf >= 0 ? make_float4(h.t, __int_as_float(h.gid), h.u, h.v)
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else {
-		stage_nodes(S, snodes, n_snodes);
+		stage_bvh(S, snodes, n_snodes);
 	}
 	const float4 *__restrict__ qa = W.qa[par];
 	const float4 *__restrict__ qb = W.qb[par];
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf, active,
 				scratch[threadIdx.x >> 5]);
 		} else if (active) {
-			h = closest_hit(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
+			h = closest_hit_any(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
 		}
 		if (active) W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 // One instantiation per closest-hit strategy (LINEAR: the staged linear scan of
 // a scene with at most LINEAR_MAX primitives, else the BVH), each with the
 // occupancy that measured fastest for it.
-template <bool LINEAR>
+template <bool LINEAR, bool WIDE = false>
 __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
 	k_tail(DevScene S, Wave W, int par) {
 	// linear scenes: the staged primitives and leaf boxes (6 float4 per primitive at most) and
@@ -230,6 +230,8 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 	if (LINEAR) {
 		stage_prims(S, snodes);
 		__syncthreads();
+	} else if (WIDE) {
+		stage_nodes4(S, snodes, n_snodes);
 	} else {
 		stage_nodes(S, snodes, n_snodes);
 	}
@@ -268,8 +270,10 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
 			bool live = true;
 			while (live) {
-				Hit hh = closest_hit<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
-					sstack + threadIdx.x);
+				Hit hh = WIDE ? closest_hit4<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
+									sstack + threadIdx.x)
+							  : closest_hit<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
+									sstack + threadIdx.x);
 				++segments;
 				live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
 					cm, q);
@@ -365,16 +369,22 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) 
 	f.height = h;
 }
 
+// the megakernel instantiation for scene S: linear scan, 4-wide tree or binary tree
+static const void *tail_fn(bool linear, const DevScene &S) {
+	if (linear) return (const void *)k_tail<true>;
+	return S.n_nodes4 > 0 ? (const void *)k_tail<false, true> : (const void *)k_tail<false, false>;
+}
+
 void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W) {
 	if (linear)
 		k_tail<true><<<grid, BLOCK, 0, s>>>(S, W, 0);
+	else if (S.n_nodes4 > 0)
+		k_tail<false, true><<<grid, BLOCK, 0, s>>>(S, W, 0);
 	else
-		k_tail<false><<<grid, BLOCK, 0, s>>>(S, W, 0);
+		k_tail<false, false><<<grid, BLOCK, 0, s>>>(S, W, 0);
 }
 
-int tail_grid(bool linear, int n_sms) {
-	return grid_for(linear ? (const void *)k_tail<true> : (const void *)k_tail<false>, n_sms);
-}
+int tail_grid(bool linear, const DevScene &S, int n_sms) { return grid_for(tail_fn(linear, S), n_sms); }
 
 void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par) {
 	if (linear)
@@ -407,7 +417,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
 	const int g_int = intersect_grid(linear, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
-	const int g_tail = tail_grid(linear, sc->n_sms);
+	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
 
 	Wave W{};
 	W.npix = p.width * p.height;

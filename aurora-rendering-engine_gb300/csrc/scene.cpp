@@ -60,6 +60,9 @@ are_status validate(const are_scene_desc *d) {
 	if (total > (int64_t)INT32_MAX / 4) return invalid("too many primitives");
 	if (d->background != ARE_BG_CONSTANT && d->background != ARE_BG_SKY_GRADIENT) return invalid("unknown background");
 	if (d->bvh_build != ARE_BVH_HOST_SAH && d->bvh_build != ARE_BVH_DEVICE) return invalid("unknown bvh_build");
+	if (d->bvh_width != 0 && d->bvh_width != 2 && d->bvh_width != 4) return invalid("bvh_width must be 0, 2 or 4");
+	if (d->bvh_width == 4 && d->bvh_build == ARE_BVH_DEVICE)
+		return invalid("bvh_width 4 needs the host build (the device build's tree is traversed two-wide)");
 	if (d->triangle_test != ARE_TRI_REFERENCE_MT && d->triangle_test != ARE_TRI_WATERTIGHT)
 		return invalid("unknown triangle test");
 	for (int32_t i = 0; i < d->n_textures; ++i) {
@@ -205,6 +208,8 @@ are_status scene_create_device(const are_scene_desc *d, are_scene **out) {
 	S.prim_mat = r.mat;
 	S.tri_uv = r.uv;
 	S.nodes = r.nodes;
+	S.nodes4 = nullptr;  // the device-built tree is traversed two-wide
+	S.n_nodes4 = 0;
 	S.leaves = nullptr;
 	S.n_leaves = 0;
 	S.n_prims = n;
@@ -303,6 +308,13 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	if (!st) st = upload(sc, mat.data(), mat.size(), &S.prim_mat);
 	if (!st) st = upload(sc, tri_uv.data(), tri_uv.size(), &S.tri_uv);
 	if (!st) st = upload(sc, (const float4 *)bvh.nodes.data(), bvh.nodes.size() / 4, &np);
+	// the 4-wide tree: measured faster for the 2M-triangle mesh (trees deep in HBM: half the dependent
+	// node fetches), slower for sphere fields of up to 152k spheres and for trees held in shared memory
+	std::vector<float> wide;
+	const bool four = d->bvh_width == 4 || (d->bvh_width == 0 && n > WIDE_BVH_MIN_PRIMS);
+	if (n > LINEAR_MAX && four) wide = collapse_bvh4(bvh, SMEM_NODES4);
+	const float4 *np4 = nullptr;
+	if (!st && !wide.empty()) st = upload(sc, (const float4 *)wide.data(), wide.size() / 4, &np4);
 	std::vector<float> leaves;
 	if (n > 0 && n <= LINEAR_MAX)
 		for (int32_t i = 0; i < bvh.n_nodes; ++i) {
@@ -323,6 +335,8 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	}
 	S.prims = pp;
 	S.nodes = np;
+	S.nodes4 = np4;
+	S.n_nodes4 = (int32_t)(wide.size() / 32);
 	S.leaves = lp;
 	S.n_leaves = (int32_t)(leaves.size() / 8);
 	S.n_prims = n;

@@ -503,7 +503,12 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 		float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax * 1.0000039f));
 		if (!(lo <= hi)) return best;
 	}
-	while (true) {
+	// a well-formed tree is walked visiting each node pair at most once
+	for (int visits = 0;; ++visits) {
+		if (visits > S.n_nodes) {
+			err |= ERR_BVH_WALK;
+			break;
+		}
 		if (b == 0) {
 			// interior: test both children (one 64-byte line)
 			int c = a;
@@ -622,6 +627,191 @@ __device__ __forceinline__ Hit closest_hit(const DevScene &S, const float4 *__re
 		if (!found) break;
 	}
 	return best;
+}
+
+
+// ---------------------------------------------------------------------------
+// 4-wide tree (DevScene::nodes4, built on the host by collapse_bvh4): each node
+// is four 32-byte child records, so one step tests four boxes from one
+// 128-byte line and the tree is half as deep as the binary one.  Same answer
+// as closest_hit: boxes only cull (padded as in the binary tree), primitives
+// are tested by the same functions and the best hit keeps the (t, global id)
+// order, whatever order the nodes are visited in.
+
+// the primitives [a, a + b) of a leaf against the best hit so far
+__device__ __forceinline__ void leaf_hits(const DevScene &S, int a, int b, f3 o, f3 d, float tmin, float tmax,
+	Hit &best) {
+	const int32_t tri_wt = S.triangle_test;
+	for (int i = a; i < a + b; ++i) {
+		const float4 *P = S.prims + 3 * (size_t)i;
+		const float4 p0 = ldg4(P);
+		float t, u = 0.0f, v = 0.0f;
+		bool h;
+		if (p0.w > 0.0f) {
+			h = hit_sphere(p0, o, d, tmin, tmax, t);
+		} else {
+			const float4 p1 = ldg4(P + 1), p2 = ldg4(P + 2);
+			if (p0.w == PRIM_TAG_QUAD)
+				h = hit_quad(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, best.t, t, u, v);
+			else if (tri_wt)
+				h = hit_tri_wt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+			else
+				h = hit_tri_mt(ld3(p0), ld3(p1), ld3(p2), o, d, tmin, tmax, t, u, v);
+		}
+		if (h && t <= best.t) {
+			const int32_t gid = __ldg(S.prim_gid + i);
+			if (t < best.t || gid < best.gid) {
+				best.t = t;
+				best.leaf = i;
+				best.gid = gid;
+				best.u = u;
+				best.v = v;
+			}
+		}
+	}
+}
+
+// Stages the first SMEM_NODES4 wide nodes (breadth-first top levels) into the
+// same 32 KB buffer stage_nodes uses.
+__device__ __forceinline__ void stage_nodes4(const DevScene &S, float4 *snodes, int &n_snodes4) {
+	n_snodes4 = min(S.n_nodes4, SMEM_NODES4);
+	for (int i = threadIdx.x; i < 8 * n_snodes4; i += blockDim.x) snodes[i] = __ldg(S.nodes4 + i);
+	__syncthreads();
+}
+
+// SHORT > 0: the first SHORT stack entries in shared memory (this thread's
+// column, entry k at sstack[k * blockDim.x]), the rest in local memory.
+template <int SHORT = 0>
+__device__ __forceinline__ Hit closest_hit4(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes4, f3 o,
+	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack = nullptr) {
+	Hit best;
+	best.t = __int_as_float(0x7f800000);
+	best.leaf = -1;
+	best.gid = 0x7fffffff;
+	best.u = best.v = 0.0f;
+	float dx = d.x != 0.0f ? d.x : copysignf(1e-20f, d.x);
+	float dy = d.y != 0.0f ? d.y : copysignf(1e-20f, d.y);
+	float dz = d.z != 0.0f ? d.z : copysignf(1e-20f, d.z);
+	float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
+	float ox = -o.x * ix, oy = -o.y * iy, oz = -o.z * iz;
+	{
+		// the root's box (binary record 0)
+		const float4 r0 = ldg4(S.nodes), r1 = ldg4(S.nodes + 1);
+		float t0x = fmaf(r0.x, ix, ox), t1x = fmaf(r1.x, ix, ox);
+		float t0y = fmaf(r0.y, iy, oy), t1y = fmaf(r1.y, iy, oy);
+		float t0z = fmaf(r0.z, iz, oz), t1z = fmaf(r1.z, iz, oz);
+		float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+		float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax * 1.0000039f));
+		if (!(lo <= hi)) return best;
+	}
+	// stack entries: (reference, count: 0 = wide node, > 0 = leaf) and the entry distance
+	int2 stack[MAX_STACK4 - SHORT];
+	float stack_t[MAX_STACK4 - SHORT];
+	int sp = 0;
+	int a = 0, b = 0;  // current entry: the root's wide node
+	const int limit = 4 * S.n_nodes4 + 1;  // a well-formed tree yields each entry once
+	for (int steps = 0;; ++steps) {
+		if (steps > limit) {
+			err |= ERR_BVH_WALK;
+			break;
+		}
+		if (b > 0) {
+			leaf_hits(S, a, b, o, d, tmin, tmax, best);
+		} else {
+			if ((unsigned)a >= (unsigned)S.n_nodes4) {
+				err |= ERR_BVH_WALK;
+				break;
+			}
+			// the four children: entry distances of those entered, nearest first
+			const bool shared = a < n_snodes4;
+			const float4 *__restrict__ src = shared ? snodes + 8 * a : S.nodes4 + 8 * (size_t)a;
+			const float bt = fminf(best.t, tmax) * 1.0000039f;
+			float l[4];
+			int2 e[4];
+#pragma unroll
+			for (int k = 0; k < 4; ++k) {
+				const float4 c0 = shared ? src[2 * k] : ldg4(src + 2 * k);
+				const float4 c1 = shared ? src[2 * k + 1] : ldg4(src + 2 * k + 1);
+				float t0x = fmaf(c0.x, ix, ox), t1x = fmaf(c1.x, ix, ox);
+				float t0y = fmaf(c0.y, iy, oy), t1y = fmaf(c1.y, iy, oy);
+				float t0z = fmaf(c0.z, iz, oz), t1z = fmaf(c1.z, iz, oz);
+				const float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+				const float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+				e[k] = make_int2(__float_as_int(c0.w), __float_as_int(c1.w));
+				// unused slots (count < 0) and boxes not entered sort last
+				l[k] = (lo <= hi && e[k].y >= 0) ? lo : __int_as_float(0x7f800000);
+			}
+			// sorting network on (l, e), ascending
+#define ARE_CSWAP(i, j)                                           \
+	if (l[j] < l[i]) {                                            \
+		const float tl = l[i];                                    \
+		l[i] = l[j], l[j] = tl;                                   \
+		const int2 te = e[i];                                     \
+		e[i] = e[j], e[j] = te;                                   \
+	}
+			ARE_CSWAP(0, 1) ARE_CSWAP(2, 3) ARE_CSWAP(0, 2) ARE_CSWAP(1, 3) ARE_CSWAP(1, 2)
+#undef ARE_CSWAP
+			// push the farther entered children (farthest first), continue with the nearest
+			const float inf = __int_as_float(0x7f800000);
+#pragma unroll
+			for (int k = 3; k >= 1; --k) {
+				if (!(l[k] < inf)) continue;
+				if (SHORT > 0 && sp < SHORT) {
+					sstack[sp++ * (int)blockDim.x] = make_int4(e[k].x, e[k].y, __float_as_int(l[k]), 0);
+				} else if (sp < MAX_STACK4) {
+					stack[sp - SHORT] = e[k];
+					stack_t[sp++ - SHORT] = l[k];
+				} else {
+					err |= ERR_STACK_OVERFLOW;
+				}
+			}
+			if (l[0] < inf) {
+				a = e[0].x;
+				b = e[0].y;
+				continue;
+			}
+		}
+		// pop, skipping entries that begin beyond the best hit found since the push
+		bool found = false;
+		while (sp > 0) {
+			--sp;
+			int2 en;
+			float te;
+			if (SHORT > 0 && sp < SHORT) {
+				const int4 r = sstack[sp * (int)blockDim.x];
+				en = make_int2(r.x, r.y);
+				te = __int_as_float(r.z);
+			} else {
+				en = stack[sp - SHORT];
+				te = stack_t[sp - SHORT];
+			}
+			if (te <= best.t * 1.0000039f) {
+				a = en.x;
+				b = en.y;
+				found = true;
+				break;
+			}
+		}
+		if (!found) break;
+	}
+	return best;
+}
+
+// Stages the top of whichever tree closest_hit_any traverses.
+__device__ __forceinline__ void stage_bvh(const DevScene &S, float4 *snodes, int &n_snodes) {
+	if (S.n_nodes4 > 0)
+		stage_nodes4(S, snodes, n_snodes);
+	else
+		stage_nodes(S, snodes, n_snodes);
+}
+
+// The 4-wide tree when the scene has one, else the binary tree; `snodes` /
+// `n_snodes` as staged by stage_bvh.
+template <int SHORT = 0>
+__device__ __forceinline__ Hit closest_hit_any(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
+	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack = nullptr) {
+	if (S.n_nodes4 > 0) return closest_hit4<SHORT>(S, snodes, n_snodes, o, d, tmin, tmax, err, sstack);
+	return closest_hit<SHORT>(S, snodes, n_snodes, o, d, tmin, tmax, err, sstack);
 }
 
 }  // namespace are_core

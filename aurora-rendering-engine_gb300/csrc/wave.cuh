@@ -54,7 +54,7 @@ __global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ v
 // k_tail (render.cu) for a scene scanned linearly (linear) or through its BVH, on queue 0;
 // tail_grid: its persistent grid (resident blocks x SMs)
 void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W);
-int tail_grid(bool linear, int n_sms);
+int tail_grid(bool linear, const DevScene &S, int n_sms);
 // k_intersect (render.cu) for a linear-scan or BVH scene on queue par, and its grid
 void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par);
 int intersect_grid(bool linear, int n_sms);

@@ -112,6 +112,8 @@ typedef struct are_scene_desc {
 	int32_t triangle_test;      /* ARE_TRI_* */
 	int32_t bvh_leaf_size;      /* max primitives per BVH leaf; 0 = default (4) */
 	int32_t bvh_build;          /* ARE_BVH_*: where the tree is built (same answers either way) */
+	int32_t bvh_width;          /* children per BVH node traversed: 0 = automatic (4 above 2^19 primitives,
+	                               else 2), 2, or 4 (host build only); same answers either way */
 } are_scene_desc;
 
 enum {
@@ -181,7 +183,9 @@ typedef struct are_render_stats {
 	double device_ms;           /* CUDA-event time of the whole render on its stream */
 	double kernel_ms[4];        /* CUDA-event time per kernel kind (ARE_KERNEL_*) */
 	int64_t kernel_launches[4]; /* launches per kernel kind */
-	int32_t error_word;         /* device error bits, 0 = clean */
+	int32_t error_word;         /* device error bits, 0 = clean: 1 traversal stack overflow, 2 path queue
+	                               overflow, 4 bad index, 8 non-finite radiance (dropped), 16 tensor-core
+	                               wait timed out, 32 BVH walk visited more nodes than the tree has */
 	int32_t reserved_;
 	double aux[4];              /* are_render: [0] segments traced by the end-of-render tail kernel;
 	                               are_render_guided: training samples, Adam steps, guided vertices, last loss */

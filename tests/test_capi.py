@@ -39,7 +39,8 @@ def _create(lib, s):
 
 
 @pytest.mark.parametrize("case", ["null_tri_material", "zero_edge", "collinear", "bad_sphere", "bad_texture",
-                                  "bad_image", "bad_mat_type", "degenerate_quad"])
+                                  "bad_image", "bad_mat_type", "degenerate_quad", "bad_bvh_width",
+                                  "wide_device_build"])
 def test_descriptor_validation(lib, case):
     """Mirrors are::Triangle's constructor checks (src/object/triangle.cpp:9-46)
     and are::Texture's size check (src/texture.cpp:52-55); validation runs
@@ -62,6 +63,10 @@ def test_descriptor_validation(lib, case):
         s.materials["type"][0] = 17
     elif case == "degenerate_quad":
         s.add_quads([0, 0, 0, 1, 0, 0, 2, 0, 0], m)
+    elif case == "bad_bvh_width":
+        s.bvh_width = 3
+    elif case == "wide_device_build":  # the device build's tree is traversed two-wide only
+        s.bvh_width, s.bvh_build = 4, are.BVH_DEVICE
     st, msg = _create(lib, s)
     assert st == 1, (case, st, msg)
     assert msg

@@ -150,3 +150,25 @@ def test_device_pointer_path(gpu_lib, oracle):
     torch.cuda.synchronize()
     sc.intersect_device(dr.data_ptr(), len(r), dh.data_ptr())
     assert_bitexact(oracle.intersect(oracle.prepare(s), r), dh.cpu().numpy(), "device ptrs")
+
+
+@pytest.mark.parametrize("cfg,kw", [(are.CONFIG_RANDOM_SPHERES, dict(lo=-12, hi=12, camera=(13, 2, 3))),
+                                    (are.CONFIG_SPHERE_FIELD, dict(lo=-12, hi=12, camera=(13, 2, 3)))])
+def test_bvh_widths_give_the_same_answers(gpu_lib, oracle, nthreads, cfg, kw):
+    """The binary and the 4-wide tree over the same scene: every closest hit
+    bit-identical (and equal to the oracle's), and the rendered image too."""
+    import dataclasses
+    s, cam, par = are.build_config(cfg, seed=7, mesh_frequency=20_000 if cfg == are.CONFIG_SPHERE_FIELD else 0)
+    s2, s4 = (are.Scene(dataclasses.replace(s, bvh_width=w)) for w in (2, 4))
+    r = random_rays(500_000, 31, t_min=1e-3, t_max=np.inf, **kw)
+    h2, _ = s2.intersect(r)
+    h4, _ = s4.intersect(r)
+    assert np.array_equal(h2.view(np.uint32), h4.view(np.uint32))
+    idx = np.arange(0, len(r), 25)
+    assert_bitexact(oracle.intersect(oracle.prepare(s), r[idx], nthreads), h4[idx], "4-wide")
+    par = dict(par, width=96, height=54, spp=8, chunk=2)
+    a, va, sa = s2.render(cam, par)
+    b, vb, sb = s4.render(cam, par)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["error_word"] == sb["error_word"] == 0
