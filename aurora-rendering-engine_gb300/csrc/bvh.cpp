@@ -420,6 +420,8 @@ std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes) {
 	std::vector<std::array<int32_t, 4>> refs;  // per wide node: wide index of each interior child, -1 otherwise
 	std::vector<std::array<int32_t, 4>> kids_of;
 	std::vector<int> nkids;
+	const size_t cap = (size_t)bvh.n_nodes / 2 + 1;  // at most one wide node per binary interior node
+	src.reserve(cap), refs.reserve(cap), kids_of.reserve(cap), nkids.reserve(cap);
 	refs.push_back({ -1, -1, -1, -1 });
 	kids_of.push_back({ -1, -1, -1, -1 });
 	nkids.push_back(0);
@@ -435,7 +437,8 @@ std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes) {
 		int32_t kids[4];
 		const int n = gather(src[w], kids);
 		nkids[w] = n;
-		std::vector<int32_t> inner;
+		int32_t inner[4];
+		int n_inner = 0;
 		for (int k = 0; k < n; ++k) {
 			kids_of[w][k] = kids[k];
 			if (is_leaf(kids[k])) continue;
@@ -445,12 +448,12 @@ std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes) {
 			kids_of.push_back({ -1, -1, -1, -1 });
 			nkids.push_back(0);
 			refs[w][k] = m;
-			inner.push_back(m);
+			inner[n_inner++] = m;
 		}
 		if ((int)src.size() < bfs_nodes) {
-			for (int32_t m : inner) work.push_back(m);
+			for (int k = 0; k < n_inner; ++k) work.push_back(inner[k]);
 		} else {  // depth-first: the first child next
-			for (auto it = inner.rbegin(); it != inner.rend(); ++it) work.push_back(*it);
+			for (int k = n_inner - 1; k >= 0; --k) work.push_back(inner[k]);
 		}
 	}
 	const size_t nw = src.size();
