@@ -84,7 +84,7 @@ __device__ __forceinline__ bool finish_path(const Wave &W, int slot, f3 L, int64
 struct PathState {
 	f3 o, d, beta, L;
 	int slot, depth, j;
-	int64_t item;
+	uint32_t item;  // work item (fewer than 2^32, checked on the host)
 };
 
 __device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i) {
@@ -94,7 +94,7 @@ __device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i)
 	P.slot = __float_as_int(ra.w);
 	const int meta = __float_as_int(rb.w);
 	P.depth = meta & 0xff, P.j = meta >> 8;
-	P.item = (int64_t)(unsigned)__float_as_int(rc.w);
+	P.item = (uint32_t)__float_as_int(rc.w);
 	return P;
 }
 
@@ -113,7 +113,7 @@ __device__ __forceinline__ void camera_path(const Wave &W, int slot, int64_t ite
 	camera_ray(W.cam, pixel % W.cam.width, pixel / W.cam.width, key, P.o, P.d);
 	P.beta = f3{ 1.f, 1.f, 1.f };
 	P.L = f3{ 0.f, 0.f, 0.f };
-	P.slot = slot, P.depth = 0, P.j = j, P.item = item;
+	P.slot = slot, P.depth = 0, P.j = j, P.item = (uint32_t)item;
 }
 
 }  // namespace are_core

@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			if (live) {
 				P = load_path(W, par, i);
 				sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
+				sm.w = cm.w = q.w = 0.f;  // unused lanes: constant, so they hold no registers in the loop
 			}
 			const int slot = P.slot;
 			while (__any_sync(0xffffffffu, live)) {
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			const int slot = P.slot;
 			// the slot's sums stay in registers while this thread owns the slot
 			float4 sm = W.acc_s[slot], cm = W.acc_c[slot], q = W.acc_q[slot];
+			sm.w = cm.w = q.w = 0.f;
 			bool live = true;
 			while (live) {
 				Hit hh = WIDE ? closest_hit4<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
