@@ -1,6 +1,6 @@
-// path.cuh — per-path pieces shared by the wavefront renderers (render.cu,
-// guided.cu): warp-aggregated appends, work-item coordinates, the 64-byte
-// queue record of a path, camera paths and the accumulate step.
+// path.cuh — per-path pieces shared by the renderers (render.cu: megakernel
+// and wavefront; guided.cu): warp-aggregated appends, work-item coordinates,
+// the 64-byte queue record of a path, camera paths and the accumulate step.
 #pragma once
 
 #include "shade.cuh"

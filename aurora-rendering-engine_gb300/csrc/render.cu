@@ -1,25 +1,28 @@
-// render.cu — the wavefront path tracer and the batched closest-hit query.
+// render.cu — the path tracer (megakernel and wavefront schedules) and the
+// batched closest-hit query.
 //
 // Replaces rt.cpp render() / trace() / intersect() (experiments/rt.cpp:209-374).
 // The reference walks pixels one by one and recurses per path on one host
-// thread.  Here a pool of P paths lives in HBM as 64-byte SoA queue records
-// (the path state travels with its ray) and every wavefront iteration runs two
-// kernels over compacted queues:
+// thread.  Here work items are (pixel, chunk of samples); a path slot runs an
+// item's samples in order and keeps their Kahan sums, so the per-item sums -
+// and the image - do not depend on scheduling; `resolve` adds the items of
+// each pixel in chunk order.  Two schedules run the slots:
 //
-//   intersect : closest hit of every queued ray (BVH with its top levels in
-//               shared memory, or a linear scan of tiny scenes)
-//   shade     : emission + material scatter + Russian roulette; a surviving
-//               path appends its next ray to the output queue; a finished
-//               path adds its radiance to its slot's Kahan sum, takes its
-//               next sample (or next work item) and appends that camera ray
-//               instead (warp-ballot compaction, one atomic per warp)
-//
-// Work items are (pixel, chunk of samples); each item's samples run in one
-// slot in order, so the per-item Kahan sums - and the image - do not depend
-// on scheduling.  `resolve` adds the items of each pixel in chunk order.
-// Iterations are captured K at a time in a CUDA graph; when every item is
-// taken and few paths remain, `tail` finishes them in one launch.  Under the
-// megakernel schedule `tail` renders the whole frame in one persistent launch.
+//   megakernel (default): `tail` as one persistent launch, one slot per
+//     resident thread; a thread traces its path to the end, accumulates it,
+//     takes its next sample or work item and goes on, the path state and the
+//     slot's sums in registers.  One instantiation per closest-hit strategy
+//     (warp-cooperative linear scan of a tiny scene; binary or 4-wide BVH).
+//   wavefront: a pool of P paths in HBM as 64-byte SoA queue records (the
+//     path state travels with its ray), two kernels per iteration over
+//     compacted queues, captured K iterations at a time in a CUDA graph:
+//       intersect : closest hit of every queued ray
+//       shade     : emission + scatter + Russian roulette; a surviving path
+//                   appends its next ray, a finished one accumulates and
+//                   appends its slot's next camera ray (warp-ballot
+//                   compaction, one atomic per warp)
+//     and, when every item is taken and few paths remain, `tail` finishes
+//     them in one launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>

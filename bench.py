@@ -673,6 +673,11 @@ def main() -> None:
         cpu = {"value": round(r["value"], 4), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{r['frames']} x {r['rows']} rows x {W} px x {r['spp']} spp of the same frame "
                          f"({r['seconds']:.1f} s)"}
+        # the same port on one thread (the reference's own render() is single-threaded)
+        r1 = cpu_sample(scene_arrays, cam, par, float(os.environ.get("ARE_CPU1_SECONDS", "5")), 1)
+        cpu["one_thread"] = {"value": round(r1["value"], 4), "cores": 1,
+                             "sample": f"{r1['frames']} x {r1['rows']} rows x {W} px x {r1['spp']} spp "
+                                       f"({r1['seconds']:.1f} s)"}
 
     if rank == 0:
         gpu_launches = sum(sum(s["kernel_launches"].values()) for s in stats)
