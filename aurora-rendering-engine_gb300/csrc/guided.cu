@@ -341,7 +341,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		carve<float>(z, 3 * (size_t)W.npix);
 	need = (size_t)z;
 	void *mem = nullptr;
-	if (are_status st = cuda_status(cudaMalloc(&mem, need), "cudaMalloc(guided render)")) return st;
+	if (are_status st = pool_alloc(sc, need, &mem)) return st;
 	z = (char *)mem;
 	for (int q = 0; q < 2; ++q)
 		W.qa[q] = carve<float4>(z, P), W.qb[q] = carve<float4>(z, P), W.qc[q] = carve<float4>(z, P),
@@ -500,7 +500,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	}
 	for (auto &e : kev) cudaEventDestroy(e);
 	cudaStreamSynchronize(s);
-	cudaFree(mem);
+	pool_free(sc, mem);
 	if (!st && herr) {
 		set_error("device error word " + std::to_string(herr));
 		st = ARE_ERR_INTERNAL;

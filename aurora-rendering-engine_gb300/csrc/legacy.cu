@@ -325,7 +325,7 @@ are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_
 	size_t npix = (size_t)p.width * p.height;
 	size_t need = 256 + (dev_out ? 0 : npix * 12) + (mt ? (size_t)624 * p.height * 4 : 0);
 	void *tmp = nullptr;
-	if (are_status st = cuda_status(cudaMalloc(&tmp, need), "cudaMalloc(legacy)")) return st;
+	if (are_status st = pool_alloc(sc, need, &tmp)) return st;
 	unsigned *err_word = (unsigned *)tmp;
 	float *d_rgb = dev_out ? rgb : (float *)((char *)tmp + 256);
 	uint32_t *mt_state = (uint32_t *)((char *)tmp + 256 + (dev_out ? 0 : npix * 12));
@@ -357,7 +357,7 @@ are_status render_legacy(are_scene *sc, const are_camera *cam, const are_render_
 	cudaEventElapsedTime(&ms, e0, e1);
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
-	cudaFree(tmp);
+	pool_free(sc, tmp);
 	if (!st && herr) {
 		set_error("device error word " + std::to_string(herr));
 		st = ARE_ERR_INTERNAL;

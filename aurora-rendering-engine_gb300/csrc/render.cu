@@ -464,18 +464,18 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	}
 	cudaStream_t s = sc->stream;
 	if (need > sc->ws_bytes) {
-		if (sc->ws) cudaFree(sc->ws);
+		pool_free(sc, sc->ws);
 		sc->ws = nullptr;
 		sc->ws_bytes = 0;
-		if (are_status st = cuda_status(cudaMalloc(&sc->ws, need), "cudaMalloc(workspace)")) return st;
+		if (are_status st = pool_alloc(sc, need, &sc->ws)) return st;
 		sc->ws_bytes = need;
 	}
 	size_t item_need = (size_t)W.n_items * 2 * sizeof(float4) + 2 * (size_t)W.npix * 3 * sizeof(float);
 	if (item_need > sc->items_bytes) {
-		if (sc->items) cudaFree(sc->items);
+		pool_free(sc, sc->items);
 		sc->items = nullptr;
 		sc->items_bytes = 0;
-		if (are_status st = cuda_status(cudaMalloc(&sc->items, item_need), "cudaMalloc(work items)")) return st;
+		if (are_status st = pool_alloc(sc, item_need, &sc->items)) return st;
 		sc->items_bytes = item_need;
 	}
 	{

@@ -8,6 +8,7 @@
 // (src/object/triangle.cpp:9-46); here those become ARE_ERR_INVALID_ARGUMENT.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -16,6 +17,96 @@
 #include "scene.h"
 
 namespace are_core {
+
+// ---- memory ----------------------------------------------------------------
+
+namespace {
+
+constexpr uint64_t POOL_KEEP_BYTES = 1ull << 30;  // cached in the pool between frees
+
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[256];
+bool g_pool_failed[256];
+
+std::mutex g_pinned_mu;
+std::vector<unsigned *> g_pinned_free;
+
+}  // namespace
+
+// Falls back to cudaMalloc (recorded in sc->allocations) if the device has no
+// pool support.
+are_status pool_alloc(are_scene *sc, size_t bytes, void **p) {
+	*p = nullptr;
+	if (bytes == 0) return ARE_OK;
+	cudaMemPool_t pool = nullptr;
+	if (sc->device >= 0 && sc->device < 256) {
+		std::lock_guard<std::mutex> lk(g_pool_mu);
+		if (!g_pools[sc->device] && !g_pool_failed[sc->device]) {
+			cudaMemPoolProps props{};
+			props.allocType = cudaMemAllocationTypePinned;
+			props.location.type = cudaMemLocationTypeDevice;
+			props.location.id = sc->device;
+			if (cudaMemPoolCreate(&g_pools[sc->device], &props) == cudaSuccess) {
+				uint64_t keep = POOL_KEEP_BYTES;
+				cudaMemPoolSetAttribute(g_pools[sc->device], cudaMemPoolAttrReleaseThreshold, &keep);
+			} else {
+				cudaGetLastError();
+				g_pools[sc->device] = nullptr;
+				g_pool_failed[sc->device] = true;
+			}
+		}
+		pool = g_pools[sc->device];
+	}
+	if (pool) {
+		if (are_status st = cuda_status(cudaMallocFromPoolAsync(p, bytes, pool, sc->stream), "cudaMallocFromPoolAsync"))
+			return st;
+		sc->pool_allocations.push_back(*p);
+		return ARE_OK;
+	}
+	if (are_status st = cuda_status(cudaMalloc(p, bytes), "cudaMalloc")) return st;
+	sc->allocations.push_back(*p);
+	return ARE_OK;
+}
+
+void pool_free(are_scene *sc, void *p) {
+	if (!p) return;
+	for (size_t i = 0; i < sc->pool_allocations.size(); ++i)
+		if (sc->pool_allocations[i] == p) {
+			cudaFreeAsync(p, sc->stream);
+			sc->pool_allocations.erase(sc->pool_allocations.begin() + (long)i);
+			return;
+		}
+	for (size_t i = 0; i < sc->allocations.size(); ++i)
+		if (sc->allocations[i] == p) {
+			cudaFree(p);
+			sc->allocations.erase(sc->allocations.begin() + (long)i);
+			return;
+		}
+}
+
+unsigned *pinned_block_acquire() {
+	std::lock_guard<std::mutex> lk(g_pinned_mu);
+	if (g_pinned_free.empty()) {
+		// a new chunk of 64 blocks; chunks live as long as the process
+		constexpr size_t BLOCK_BYTES = 256, BLOCKS = 64;
+		unsigned char *chunk = nullptr;
+		if (cudaMallocHost((void **)&chunk, BLOCK_BYTES * BLOCKS) != cudaSuccess) {
+			cudaGetLastError();
+			return nullptr;
+		}
+		for (size_t k = 0; k < BLOCKS; ++k) g_pinned_free.push_back((unsigned *)(chunk + BLOCK_BYTES * k));
+	}
+	unsigned *p = g_pinned_free.back();
+	g_pinned_free.pop_back();
+	return p;
+}
+
+void pinned_block_release(unsigned *p) {
+	if (!p) return;
+	std::lock_guard<std::mutex> lk(g_pinned_mu);
+	g_pinned_free.push_back(p);
+}
+
 
 static thread_local std::string g_err;
 void set_error(const std::string &msg) { g_err = msg; }
@@ -198,7 +289,10 @@ are_status scene_create_device(const are_scene_desc *d, are_scene **out) {
 	if (!st) st = upload(sc, (const DevMaterial *)d->materials, (size_t)d->n_materials, &S.mats);
 	if (!st) st = upload(sc, (const DevTexture *)d->textures, (size_t)d->n_textures, &S.texs);
 	if (!st) st = upload(sc, d->texels, 3 * (size_t)d->n_texels, &S.texels);
-	if (!st) st = cuda_status(cudaMallocHost((void **)&sc->host_counters, 64 * sizeof(unsigned)), "cudaMallocHost");
+	if (!st && !(sc->host_counters = pinned_block_acquire())) {
+		set_error("pinned host memory for the render counters");
+		st = ARE_ERR_OUT_OF_MEMORY;
+	}
 	if (st) {
 		delete sc;
 		return st;
@@ -297,24 +391,11 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 		}
 	}
 
-	are_scene *sc = new are_scene();
-	cudaGetDevice(&sc->device);
-	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
-	are_status st = ARE_OK;
-	DevScene &S = sc->dev;
-	const float4 *pp = nullptr, *np = nullptr;
-	if (!st) st = upload(sc, (const float4 *)prims.data(), prims.size() / 4, &pp);
-	if (!st) st = upload(sc, gid.data(), gid.size(), &S.prim_gid);
-	if (!st) st = upload(sc, mat.data(), mat.size(), &S.prim_mat);
-	if (!st) st = upload(sc, tri_uv.data(), tri_uv.size(), &S.tri_uv);
-	if (!st) st = upload(sc, (const float4 *)bvh.nodes.data(), bvh.nodes.size() / 4, &np);
 	// the 4-wide tree: measured faster for the 2M-triangle mesh (trees deep in HBM: half the dependent
 	// node fetches), slower for sphere fields of up to 152k spheres and for trees held in shared memory
 	std::vector<float> wide;
 	const bool four = d->bvh_width == 4 || (d->bvh_width == 0 && n > WIDE_BVH_MIN_PRIMS);
 	if (n > LINEAR_MAX && four) wide = collapse_bvh4(bvh, SMEM_NODES4);
-	const float4 *np4 = nullptr;
-	if (!st && !wide.empty()) st = upload(sc, (const float4 *)wide.data(), wide.size() / 4, &np4);
 	std::vector<float> leaves;
 	if (n > 0 && n <= LINEAR_MAX)
 		for (int32_t i = 0; i < bvh.n_nodes; ++i) {
@@ -322,17 +403,56 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 			std::memcpy(&cnt, &bvh.nodes[8 * (size_t)i + 7], 4);
 			if (cnt > 0) leaves.insert(leaves.end(), &bvh.nodes[8 * (size_t)i], &bvh.nodes[8 * (size_t)i] + 8);
 		}
-	const float4 *lp = nullptr;
-	if (!st) st = upload(sc, (const float4 *)leaves.data(), leaves.size() / 4, &lp);
-	if (!st) st = upload(sc, (const DevMaterial *)d->materials, (size_t)d->n_materials, &S.mats);
-	if (!st) st = upload(sc, (const DevTexture *)d->textures, (size_t)d->n_textures, &S.texs);
-	if (!st) st = upload(sc, d->texels, 3 * (size_t)d->n_texels, &S.texels);
-	if (!st) st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-	if (!st) st = cuda_status(cudaMallocHost((void **)&sc->host_counters, 64 * sizeof(unsigned)), "cudaMallocHost");
+
+	are_scene *sc = new are_scene();
+	cudaGetDevice(&sc->device);
+	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
+	DevScene &S = sc->dev;
+	are_status st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	if (!st && !(sc->host_counters = pinned_block_acquire())) {
+		set_error("pinned host memory for the render counters");
+		st = ARE_ERR_OUT_OF_MEMORY;
+	}
+	// every array of the scene in one block from the device's pool, at 256-byte offsets, copied on the
+	// scene's stream (one allocation and one synchronisation per scene)
+	struct Part {
+		const void *src;
+		size_t bytes;
+		size_t off;
+	};
+	Part parts[] = { { prims.data(), prims.size() * 4, 0 }, { gid.data(), gid.size() * 4, 0 },
+		{ mat.data(), mat.size() * 4, 0 }, { tri_uv.data(), tri_uv.size() * 4, 0 },
+		{ bvh.nodes.data(), bvh.nodes.size() * 4, 0 }, { wide.data(), wide.size() * 4, 0 },
+		{ leaves.data(), leaves.size() * 4, 0 }, { d->materials, sizeof(DevMaterial) * (size_t)d->n_materials, 0 },
+		{ d->textures, sizeof(DevTexture) * (size_t)d->n_textures, 0 }, { d->texels, 12 * (size_t)d->n_texels, 0 } };
+	static_assert(sizeof(DevMaterial) == sizeof(are_material) && sizeof(DevTexture) == sizeof(are_texture),
+		"device records mirror the descriptor's");
+	size_t total = 0;
+	for (Part &q : parts) {
+		q.off = total;
+		total += (q.bytes + 255) & ~(size_t)255;
+	}
+	char *block = nullptr;
+	if (!st) st = pool_alloc(sc, total, (void **)&block);
+	for (Part &q : parts) {
+		if (st) break;
+		if (q.bytes) st = cuda_status(cudaMemcpyAsync(block + q.off, q.src, q.bytes, cudaMemcpyHostToDevice, sc->stream),
+						  "scene upload");
+	}
+	if (!st) st = cuda_status(cudaStreamSynchronize(sc->stream), "scene upload");
 	if (st) {
 		delete sc;
 		return st;
 	}
+	auto at = [&](int k) -> const void * { return parts[k].bytes ? block + parts[k].off : nullptr; };
+	const float4 *pp = (const float4 *)at(0), *np = (const float4 *)at(4), *np4 = (const float4 *)at(5);
+	const float4 *lp = (const float4 *)at(6);
+	S.prim_gid = (const int32_t *)at(1);
+	S.prim_mat = (const int32_t *)at(2);
+	S.tri_uv = (const float *)at(3);
+	S.mats = (const DevMaterial *)at(7);
+	S.texs = (const DevTexture *)at(8);
+	S.texels = (const float *)at(9);
 	S.prims = pp;
 	S.nodes = np;
 	S.nodes4 = np4;
@@ -368,8 +488,8 @@ are_scene::~are_scene() {
 	if (render_exec) cudaGraphExecDestroy(render_exec);
 	for (cudaEvent_t e : render_events) cudaEventDestroy(e);
 	for (void *p : allocations) cudaFree(p);
-	if (ws) cudaFree(ws);
-	if (items) cudaFree(items);
-	if (host_counters) cudaFreeHost(host_counters);
+	// pool blocks (the scene arrays, the render workspace) go back to the pool in stream order
+	for (void *p : pool_allocations) cudaFreeAsync(p, stream);
+	are_core::pinned_block_release(host_counters);
 	if (stream) cudaStreamDestroy(stream);
 }

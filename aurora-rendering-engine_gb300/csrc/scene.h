@@ -18,7 +18,8 @@ struct are_scene {
 	int32_t n_spheres = 0, n_quads = 0, n_triangles = 0;
 	int32_t max_leaf = 0, depth = 0;
 	float box_lo[3] = { 0, 0, 0 }, box_hi[3] = { 0, 0, 0 };  // bounds of all primitives
-	std::vector<void *> allocations;  // device buffers owned by the scene
+	std::vector<void *> allocations;       // device buffers owned by the scene (cudaMalloc)
+	std::vector<void *> pool_allocations;  // device buffers from the device's pool (freed on `stream`)
 	cudaStream_t stream = nullptr;
 
 	// cached wavefront workspace (grown on demand)
@@ -26,7 +27,7 @@ struct are_scene {
 	size_t ws_bytes = 0;
 	void *items = nullptr;
 	size_t items_bytes = 0;
-	unsigned *host_counters = nullptr;  // pinned
+	unsigned *host_counters = nullptr;  // pinned (a block of the process-wide slab)
 
 	// the render's CUDA graph and timing events, kept between renders: a new
 	// render updates the instantiated graph in place (same topology, new
@@ -45,6 +46,17 @@ const char *last_error();
 
 // CUDA call guard: records a message and returns ARE_ERR_CUDA / ARE_ERR_OUT_OF_MEMORY
 are_status cuda_status(cudaError_t e, const char *what);
+
+// Memory.  Scene arrays and render workspaces come from one stream-ordered
+// pool per device (cudaMemPool) that keeps up to 1 GiB cached after frees, so a
+// caller that creates, renders and destroys a scene per frame does not pay
+// cudaMalloc and cudaFree (each a device-wide synchronisation) every time.
+// Allocations are ordered on the scene's stream; pool_free releases on it.
+are_status pool_alloc(are_scene *sc, size_t bytes, void **p);
+void pool_free(are_scene *sc, void *p);
+// 256-byte pinned host blocks (read-back counters) from a process-wide slab
+unsigned *pinned_block_acquire();
+void pinned_block_release(unsigned *p);
 
 are_status scene_create(const are_scene_desc *desc, are_scene **out);
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *p, float *rgb, float *var,
