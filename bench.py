@@ -216,23 +216,36 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
         out = fn()
         return out, time.perf_counter() - t
 
-    # calibrate seconds per sample of each method
-    _, tg = timed(lambda: sc.render_guided(are.Guide(seed=90), cam, dict(par, spp=256, seed=90), gp, with_var=False))
-    _, tp = timed(lambda: sc.render(cam, dict(par, spp=256, seed=91), with_var=False))
-    spp_g = max(1, int(budget_s / (tg / 256)))
-    spp_p = max(1, int(budget_s / (tp / 256)))
-    (pi, _, _), t_p = timed(lambda: sc.render(cam, dict(par, spp=spp_p, seed=2), with_var=False))
+    def plain(spp):
+        return sc.render(cam, dict(par, spp=spp, seed=2), with_var=False)
+
+    def guided_cold(spp, seed=1):
+        return sc.render_guided(are.Guide(seed=seed), cam, dict(par, spp=spp, seed=1), gp, with_var=False)
+
+    def fit(run, spp0=512):
+        # seconds per sample from a warmed call (the first pays one-time set-up), then spp for the
+        # budget; one correction if the budgeted render itself misses the budget by more than 10 %
+        run(spp0)
+        _, t0 = timed(lambda: run(spp0))
+        spp = max(1, int(budget_s / (t0 / spp0)))
+        res_, t = timed(lambda: run(spp))
+        if abs(t - budget_s) > 0.1 * budget_s:
+            spp = max(1, int(spp * budget_s / t))
+            res_, t = timed(lambda: run(spp))
+        return res_, t, spp
+
+    (pi, _, _), t_p, spp_p = fit(plain)
     ep = relmse(pi)
     out = {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]), "budget_s": budget_s,
            "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)}}
-    g = are.Guide(seed=1)
-    (gi, _, gst), t_g = timed(lambda: sc.render_guided(g, cam, dict(par, spp=spp_g, seed=1), gp, with_var=False))
+    (gi, _, gst), t_g, spp_g = fit(guided_cold)
     eg = relmse(gi)
+    g = are.Guide(seed=1)  # the cold network again, trained on from here for the warm start
     out["guided_cold"] = {"spp": spp_g, "seconds": round(t_g, 3), "relmse": round(eg, 6),
                           "adam_steps": gst["train_steps"], "relmse_plain_over_guided": round(ep / eg, 3)}
-    # warm start: the same network after six more 1024-spp renders of training
+    # warm start: a network after seven 1024-spp renders of training
     t = time.perf_counter()
-    for k in range(6):
+    for k in range(7):
         sc.render_guided(g, cam, dict(par, spp=1024, seed=100 + k), gp, with_var=False)
     t_train = time.perf_counter() - t
     (gw, _, wst), t_w = timed(lambda: sc.render_guided(g, cam, dict(par, spp=spp_g, seed=3), gp, with_var=False))
