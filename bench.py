@@ -185,7 +185,7 @@ def cpu_sample(scene, cam, par, budget_s: float, threads: int) -> dict:
             "segments": segments, "frames": frames}
 
 
-def guiding_eval(budget_s: float = 0.1) -> dict | None:
+def guiding_eval(budget_s: float = 0.1, guide_depth: int = 3, mix: float = 0.5) -> dict | None:
     """Equal-time relMSE of guided vs plain rendering on the occluded-light
     Cornell box (200x200, depth 16) against the FP64 65,536-spp CPU reference
     in tests/golden/guiding_reference_200.npz.  Each method gets the same
@@ -206,7 +206,7 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
     s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
     par = dict(par, width=res, height=res)
     sc = are.Scene(s)
-    gp = are.GuideParams.make(guide_depth=3, batch=1 << 14, train=2)
+    gp = are.GuideParams.make(guide_depth=guide_depth, mix=mix, batch=1 << 14, train=2)
 
     def relmse(img):
         return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
@@ -237,6 +237,7 @@ def guiding_eval(budget_s: float = 0.1) -> dict | None:
     (pi, _, _), t_p, spp_p = fit(plain)
     ep = relmse(pi)
     out = {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]), "budget_s": budget_s,
+           "guide_depth": guide_depth, "mix": mix,
            "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)}}
     (gi, _, gst), t_g, spp_g = fit(guided_cold)
     eg = relmse(gi)
