@@ -49,9 +49,14 @@ struct Builder {
 	// chunk-local results that the caller merges with order-free operations
 	// (min, max, sums of integers), so the result does not depend on timing.
 	static constexpr int32_t PAR_RANGE = 1 << 17;
+	// set on pool threads that each take whole jobs: their passes run inline
+	static bool &inline_passes() {
+		static thread_local bool v = false;
+		return v;
+	}
 	template <class F>
 	static int chunked(int32_t first, int32_t count, F fn) {
-		if (count < PAR_RANGE) {
+		if (count < PAR_RANGE || inline_passes()) {
 			fn(first, first + count, 0);
 			return 1;
 		}
@@ -67,6 +72,45 @@ struct Builder {
 		fn(first, first + (int32_t)(count / nc), 0);
 		for (std::thread &t : pool) t.join();
 		return nc;
+	}
+
+	// Order-preserving partition of idx[first, first + count) by `left` on the
+	// chunks of chunked(): each chunk counts its left elements, then scatters
+	// both sides to their offsets in a copy.  Returns the first right index.
+	// The chunks are fixed by the range alone, so the result does not depend
+	// on timing.
+	template <class Pred>
+	int32_t partition_parallel(int32_t first, int32_t count, Pred left) {
+		int32_t nleft[32] = { 0 };
+		const int nc = chunked(first, count, [&](int32_t b0, int32_t b1, int c) {
+			int32_t k = 0;
+			for (int32_t i = b0; i < b1; ++i) k += left(idx[i]) ? 1 : 0;
+			nleft[c] = k;
+		});
+		// chunk c covers [first + count c / nc, first + count (c + 1) / nc)
+		int32_t lofs[32], rofs[32];
+		int32_t total_left = 0;
+		for (int c = 0; c < nc; ++c) total_left += nleft[c];
+		int32_t l = first, r = first + total_left;
+		for (int c = 0; c < nc; ++c) {
+			const int32_t b0 = first + (int32_t)((int64_t)count * c / nc), b1 = first + (int32_t)((int64_t)count * (c + 1) / nc);
+			lofs[c] = l, rofs[c] = r;
+			l += nleft[c];
+			r += (b1 - b0) - nleft[c];
+		}
+		std::vector<int32_t> out((size_t)count);
+		chunked(first, count, [&](int32_t b0, int32_t b1, int c) {
+			int32_t lo_ = lofs[c] - first, ro_ = rofs[c] - first;
+			for (int32_t i = b0; i < b1; ++i) {
+				const int32_t p = idx[i];
+				if (left(p))
+					out[lo_++] = p;
+				else
+					out[ro_++] = p;
+			}
+		});
+		std::copy(out.begin(), out.end(), idx.begin() + first);
+		return first + total_left;
 	}
 
 	void bounds(int32_t first, int32_t count, double lo[3], double hi[3], double clo[3], double chi[3]) const {
@@ -189,9 +233,14 @@ struct Builder {
 		double split_cost = parent > 0 ? 0.5 + best / parent : std::numeric_limits<double>::infinity();
 		if (best_b < 0) return count <= leaf_size ? -1 : median();
 		if (count <= leaf_size && split_cost >= leaf_cost) return -1;
-		auto it = std::partition(idx.begin() + first, idx.begin() + first + count,
-			[&](int32_t p) { return bin_of(p) < best_b; });
-		int32_t mid = (int32_t)(it - idx.begin());
+		int32_t mid;
+		if (count >= PAR_RANGE) {
+			mid = partition_parallel(first, count, [&](int32_t p) { return bin_of(p) < best_b; });
+		} else {
+			auto it = std::partition(idx.begin() + first, idx.begin() + first + count,
+				[&](int32_t p) { return bin_of(p) < best_b; });
+			mid = (int32_t)(it - idx.begin());
+		}
 		if (mid == first || mid == first + count) return median();
 		return mid;
 	}
@@ -207,29 +256,76 @@ struct Builder {
 		struct Job {
 			int32_t node, first, count, depth;
 		};
-		std::vector<Job> stack;
-		nodes.push_back(TmpNode{});
-		stack.push_back({ 0, 0, n, 0 });
-		// Large subtrees are split here; subtrees below par_min primitives are
-		// set aside and built by worker threads, each into its own node list,
-		// then appended.  Every split depends only on the subtree's own
-		// primitives, so the tree is the one a single thread would build.
-		const int32_t par_min = std::max<int32_t>(4096, n / 256);
+		// The top of the tree is split level by level.  A level's jobs (disjoint
+		// ranges of idx) are split in parallel, whole jobs per thread, once there
+		// are enough of them; before that one at a time with chunk-parallel
+		// passes.  Children are then allocated in job order.  Subtrees below
+		// par_min primitives are set aside and built by worker threads, each into
+		// its own node list, then appended.  Every split depends only on the
+		// subtree's own primitives, so the tree is the one a single thread builds.
+		static const int hw_threads = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+		const int32_t par_min = std::max<int32_t>(4096, n / (4 * hw_threads));
 		std::vector<Job> deferred;
-		while (!stack.empty()) {
-			Job j = stack.back();
-			stack.pop_back();
-			if (j.count < par_min && j.count > leaf_size) {
-				deferred.push_back(j);
-				continue;
+		std::vector<Job> level{ { 0, 0, n, 0 } };
+		nodes.push_back(TmpNode{});
+		while (!level.empty()) {
+			std::vector<int32_t> mids(level.size());
+			auto split_job = [&](size_t k) {
+				const Job &j = level[k];
+				double lo[3], hi[3], clo[3], chi[3];
+				bounds(j.first, j.count, lo, hi, clo, chi);
+				TmpNode &t = nodes[j.node];
+				std::memcpy(t.lo, lo, sizeof lo);
+				std::memcpy(t.hi, hi, sizeof hi);
+				t.depth = j.depth;
+				mids[k] = split(j.first, j.count, j.depth, lo, hi, clo, chi);
+			};
+			if ((int)level.size() >= hw_threads) {
+				std::atomic<size_t> next{ 0 };
+				auto worker = [&]() {
+					inline_passes() = true;
+					for (size_t k; (k = next.fetch_add(1)) < level.size();) split_job(k);
+					inline_passes() = false;
+				};
+				std::vector<std::thread> pool;
+				for (int t = 1; t < hw_threads; ++t) pool.emplace_back(worker);
+				worker();
+				for (std::thread &t : pool) t.join();
+			} else {
+				for (size_t k = 0; k < level.size(); ++k) split_job(k);
 			}
-			expand(j, nodes, stack, max_depth);
+			std::vector<Job> below;
+			for (size_t k = 0; k < level.size(); ++k) {
+				const Job &j = level[k];
+				max_depth = std::max(max_depth, j.depth);
+				const int32_t mid = mids[k];
+				if (mid < 0) {
+					nodes[j.node].first = j.first;
+					nodes[j.node].count = j.count;
+					continue;
+				}
+				const int32_t l = (int32_t)nodes.size();
+				nodes.push_back(TmpNode{});
+				nodes.push_back(TmpNode{});
+				nodes[j.node].left = l;
+				nodes[j.node].right = l + 1;
+				const Job kids[2] = { { l, j.first, mid - j.first, j.depth + 1 },
+					{ l + 1, mid, j.first + j.count - mid, j.depth + 1 } };
+				for (const Job &c : kids) {
+					if (c.count < par_min && c.count > leaf_size)
+						deferred.push_back(c);
+					else
+						below.push_back(c);
+				}
+			}
+			level.swap(below);
 		}
 		if (deferred.empty()) return;
 		std::vector<std::vector<TmpNode>> local(deferred.size());
 		std::vector<int> local_depth(deferred.size(), 0);
 		std::atomic<size_t> next_job{ 0 };
 		auto worker = [&]() {
+			inline_passes() = true;  // whole subtrees per thread
 			for (size_t k; (k = next_job.fetch_add(1)) < deferred.size();) {
 				std::vector<TmpNode> &ln = local[k];
 				std::vector<Job> st;
@@ -241,6 +337,7 @@ struct Builder {
 					expand(j, ln, st, local_depth[k]);
 				}
 			}
+			inline_passes() = false;
 		};
 		const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
 		const unsigned nthreads = (unsigned)std::min<size_t>(hw, deferred.size());
@@ -347,33 +444,45 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 	// padding node 1: inverted box, never hit
 	for (int k = 0; k < 3; ++k) r.nodes[8 + k] = 1.0f, r.nodes[12 + k] = -1.0f;
 
-	// leaves keep the primitive ranges of the build order
+	// leaves keep the primitive ranges of the build order; node records are
+	// written in parallel ranges (each node independently)
 	r.order = b.idx;
-	int32_t max_leaf = 0;
-	for (size_t t = 0; t < ntmp; ++t) {
-		const TmpNode &tn = b.nodes[t];
-		float *o = &r.nodes[8 * (size_t)slot[t]];
-		for (int k = 0; k < 3; ++k) {
-			float lo = (float)tn.lo[k], hi = (float)tn.hi[k];
-			if ((double)lo > tn.lo[k]) lo = std::nextafter(lo, -INFINITY);
-			if ((double)hi < tn.hi[k]) hi = std::nextafter(hi, INFINITY);
-			o[k] = lo - r.box_pad;
-			o[4 + k] = hi + r.box_pad;
+	const unsigned nthreads =
+		ntmp < ((size_t)1 << 16) ? 1u : std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+	std::vector<int32_t> part_max_leaf(nthreads, 0);
+	auto write_range = [&](unsigned part) {
+		int32_t &max_leaf = part_max_leaf[part];
+		for (size_t t = ntmp * part / nthreads; t < ntmp * (part + 1) / nthreads; ++t) {
+			const TmpNode &tn = b.nodes[t];
+			float *o = &r.nodes[8 * (size_t)slot[t]];
+			for (int k = 0; k < 3; ++k) {
+				float lo = (float)tn.lo[k], hi = (float)tn.hi[k];
+				if ((double)lo > tn.lo[k]) lo = std::nextafter(lo, -INFINITY);
+				if ((double)hi < tn.hi[k]) hi = std::nextafter(hi, INFINITY);
+				o[k] = lo - r.box_pad;
+				o[4 + k] = hi + r.box_pad;
+			}
+			int32_t a, bb;
+			if (tn.left < 0) {
+				a = tn.first;
+				bb = tn.count;
+				max_leaf = std::max(max_leaf, tn.count);
+			} else {
+				a = slot[tn.left];
+				bb = 0;
+			}
+			std::memcpy(&o[3], &a, 4);
+			std::memcpy(&o[7], &bb, 4);
 		}
-		int32_t a, bb;
-		if (tn.left < 0) {
-			a = tn.first;
-			bb = tn.count;
-			max_leaf = std::max(max_leaf, tn.count);
-		} else {
-			a = slot[tn.left];
-			bb = 0;
-		}
-		std::memcpy(&o[3], &a, 4);
-		std::memcpy(&o[7], &bb, 4);
+	};
+	{
+		std::vector<std::thread> pool;
+		for (unsigned t = 1; t < nthreads; ++t) pool.emplace_back(write_range, t);
+		write_range(0);
+		for (std::thread &t : pool) t.join();
 	}
 	r.depth = b.max_depth;
-	r.max_leaf = max_leaf;
+	r.max_leaf = *std::max_element(part_max_leaf.begin(), part_max_leaf.end());
 	return r;
 }
 

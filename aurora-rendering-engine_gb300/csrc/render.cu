@@ -225,8 +225,9 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 	// one closest-hit scratch per warp; BVH scenes: the top BVH levels
 	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
 	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
-	// BVH scenes: the top TAIL_SHORT_STACK traversal-stack entries of every thread
-	__shared__ int4 sstack[LINEAR ? 1 : TAIL_SHORT_STACK * BLOCK];
+	// BVH scenes: the top traversal-stack entries of every thread
+	constexpr int SHORT = WIDE ? TAIL_SHORT_STACK_WIDE : TAIL_SHORT_STACK;
+	__shared__ int4 sstack[LINEAR ? 1 : SHORT * BLOCK];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if ((unsigned)(blockIdx.x * blockDim.x) >= n) return;
@@ -275,10 +276,8 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			sm.w = cm.w = q.w = 0.f;
 			bool live = true;
 			while (live) {
-				Hit hh = WIDE ? closest_hit4<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
-									sstack + threadIdx.x)
-							  : closest_hit<TAIL_SHORT_STACK>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err,
-									sstack + threadIdx.x);
+				Hit hh = WIDE ? closest_hit4<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x)
+							  : closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
 				++segments;
 				live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
 					cm, q);

@@ -16,7 +16,8 @@ constexpr int BLOCK = 256;
 // linear-scan scenes run best at 4 (64 registers), BVH scenes at 2 (deeper traversal state)
 constexpr int TAIL_MIN_BLOCKS_LINEAR = 4;
 constexpr int TAIL_MIN_BLOCKS_BVH = 2;
-constexpr int TAIL_SHORT_STACK = 8;  // BVH traversal-stack entries per thread kept in shared memory
+constexpr int TAIL_SHORT_STACK = 8;       // binary-tree traversal-stack entries per thread in shared memory
+constexpr int TAIL_SHORT_STACK_WIDE = 8;  // the same for the 4-wide tree
 
 struct Wave {
 	// Ray queues: one 64-byte record per queued path segment, SoA over 4 float4:

@@ -100,3 +100,29 @@ def test_linear_scan_limit(gpu_lib, oracle, nthreads, n):
     sd = np.sqrt(var + vc)
     out = (sd > 0) & (np.abs(img - mc) > 4 * sd)
     assert out.mean() < 0.01, out.mean()
+
+
+def test_scene_churn_reuses_pooled_memory(gpu_lib):
+    """Create, render and destroy a scene again and again (as a caller that
+    rebuilds its scene every frame): scene arrays and render workspaces come
+    from the device's memory pool, so after the first cycle the device's free
+    memory stays where it is — nothing leaks and nothing is allocated anew."""
+    torch = pytest.importorskip("torch")
+    s, cam, par = are.build_config(are.CONFIG_RANDOM_SPHERES)
+    par = dict(par, width=160, height=90, spp=4)
+
+    def cycle(seed):
+        sc = are.Scene(s)
+        img, _, st = sc.render(cam, dict(par, seed=seed), with_var=False)
+        sc.close()
+        assert st["error_word"] == 0 and np.isfinite(img).all()
+
+    torch.cuda.init()
+    cycle(0)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for k in range(1, 21):
+        cycle(k)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
