@@ -315,6 +315,7 @@ def load(path: str | os.PathLike | None = None):
     L.are_last_error.restype = C.c_char_p
     L.are_version.restype = C.c_int32
     L.are_device_count.restype = C.c_int32
+    L.are_trim_memory.argtypes = [C.c_int32]
     L.are_scene_create.argtypes = [C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]
     L.are_scene_destroy.argtypes = [C.c_void_p]
     L.are_scene_info.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32),
@@ -368,6 +369,11 @@ def check(status: int) -> None:
 
 # ---------------------------------------------------------------------------
 # high-level wrappers
+
+
+def trim_memory(device: int = -1) -> None:
+    """are_trim_memory: return the device memory pool's cached blocks to the driver."""
+    check(load().are_trim_memory(device))
 
 
 def build_config(config: int, seed: int = 42, mesh_frequency: int = 0):

@@ -27,6 +27,7 @@ struct TmpNode {
 };
 
 constexpr int NBINS = 16;
+constexpr int32_t SEQUENTIAL_BUILD_MAX = 1 << 15;  // primitives below which one thread builds the tree
 
 inline double area(const double lo[3], const double hi[3]) {
 	double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
@@ -256,6 +257,17 @@ struct Builder {
 		struct Job {
 			int32_t node, first, count, depth;
 		};
+		if (n < SEQUENTIAL_BUILD_MAX) {
+			// small scenes: the whole tree on this thread (starting threads would cost more)
+			std::vector<Job> st{ { 0, 0, n, 0 } };
+			nodes.push_back(TmpNode{});
+			while (!st.empty()) {
+				Job j = st.back();
+				st.pop_back();
+				expand(j, nodes, st, max_depth);
+			}
+			return;
+		}
 		// The top of the tree is split level by level.  A level's jobs (disjoint
 		// ranges of idx) are split in parallel, whole jobs per thread, once there
 		// are enough of them; before that one at a time with chunk-parallel

@@ -63,6 +63,10 @@ ARE_API int32_t are_device_count(void) {
 	return n;
 }
 
+ARE_API are_status are_trim_memory(int32_t device) {
+	return guarded([&] { return are_core::pool_trim(device); });
+}
+
 ARE_API are_status are_scene_create(const are_scene_desc *desc, are_scene **out) {
 	return guarded([&] { return are_core::scene_create(desc, out); });
 }

@@ -494,9 +494,12 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	const bool dev_out = (p.flags & ARE_FLAG_DEVICE_OUTPUT) != 0;
 
 	// timing events: ev0, ev1 around the render, then 4 per graph iteration (created once per scene)
-	if (sc->render_events.empty()) {
-		sc->render_events.resize(2 + 4 * GRAPH_ITERS);
-		for (auto &e : sc->render_events) cudaEventCreate(&e);
+	// the megakernel times two spans (render, launch), the wavefront four per graph iteration
+	const size_t n_events = mega ? 4 : 2 + 4 * GRAPH_ITERS;
+	while (sc->render_events.size() < n_events) {
+		cudaEvent_t e = nullptr;
+		cudaEventCreate(&e);
+		sc->render_events.push_back(e);
 	}
 	cudaEvent_t ev0 = sc->render_events[0], ev1 = sc->render_events[1];
 	cudaEvent_t *kev = sc->render_events.data() + 2;

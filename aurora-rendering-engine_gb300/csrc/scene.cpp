@@ -31,6 +31,12 @@ bool g_pool_failed[256];
 std::mutex g_pinned_mu;
 std::vector<unsigned *> g_pinned_free;
 
+// small scenes are uploaded through one pinned staging buffer: one copy instead of one per array
+constexpr size_t STAGE_BYTES = 8u << 20;
+std::mutex g_stage_mu;
+unsigned char *g_stage = nullptr;
+bool g_stage_failed = false;
+
 }  // namespace
 
 // Falls back to cudaMalloc (recorded in sc->allocations) if the device has no
@@ -82,6 +88,25 @@ void pool_free(are_scene *sc, void *p) {
 			sc->allocations.erase(sc->allocations.begin() + (long)i);
 			return;
 		}
+}
+
+are_status pool_trim(int device) {
+	if (device < -1 || device >= 256) {
+		set_error("device ordinal out of range");
+		return ARE_ERR_INVALID_ARGUMENT;
+	}
+	std::lock_guard<std::mutex> lk(g_pool_mu);
+	for (int d = device < 0 ? 0 : device; d < (device < 0 ? 256 : device + 1); ++d) {
+		if (!g_pools[d]) continue;
+		// frees are stream-ordered: let them land before trimming
+		int cur = 0;
+		cudaGetDevice(&cur);
+		cudaSetDevice(d);
+		cudaDeviceSynchronize();
+		cudaSetDevice(cur);
+		if (are_status st = cuda_status(cudaMemPoolTrimTo(g_pools[d], 0), "cudaMemPoolTrimTo")) return st;
+	}
+	return ARE_OK;
 }
 
 unsigned *pinned_block_acquire() {
@@ -434,12 +459,28 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	}
 	char *block = nullptr;
 	if (!st) st = pool_alloc(sc, total, (void **)&block);
+	bool staged = false;
+	if (!st && total <= STAGE_BYTES) {
+		std::lock_guard<std::mutex> lk(g_stage_mu);
+		if (!g_stage && !g_stage_failed && cudaMallocHost((void **)&g_stage, STAGE_BYTES) != cudaSuccess) {
+			cudaGetLastError();
+			g_stage = nullptr;
+			g_stage_failed = true;
+		}
+		if (g_stage) {
+			for (const Part &q : parts)
+				if (q.bytes) std::memcpy(g_stage + q.off, q.src, q.bytes);
+			st = cuda_status(cudaMemcpyAsync(block, g_stage, total, cudaMemcpyHostToDevice, sc->stream), "scene upload");
+			if (!st) st = cuda_status(cudaStreamSynchronize(sc->stream), "scene upload");  // the buffer is reused
+			staged = true;
+		}
+	}
 	for (Part &q : parts) {
-		if (st) break;
+		if (st || staged) break;
 		if (q.bytes) st = cuda_status(cudaMemcpyAsync(block + q.off, q.src, q.bytes, cudaMemcpyHostToDevice, sc->stream),
 						  "scene upload");
 	}
-	if (!st) st = cuda_status(cudaStreamSynchronize(sc->stream), "scene upload");
+	if (!st && !staged) st = cuda_status(cudaStreamSynchronize(sc->stream), "scene upload");
 	if (st) {
 		delete sc;
 		return st;

@@ -54,6 +54,8 @@ are_status cuda_status(cudaError_t e, const char *what);
 // Allocations are ordered on the scene's stream; pool_free releases on it.
 are_status pool_alloc(are_scene *sc, size_t bytes, void **p);
 void pool_free(are_scene *sc, void *p);
+// releases the cached (unused) memory of device's pool, or of every pool for -1
+are_status pool_trim(int device);
 // 256-byte pinned host blocks (read-back counters) from a process-wide slab
 unsigned *pinned_block_acquire();
 void pinned_block_release(unsigned *p);

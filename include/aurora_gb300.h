@@ -200,6 +200,11 @@ ARE_API const char *are_last_error(void);
 ARE_API int32_t are_version(void);
 /* Number of CUDA devices visible (0 when no GPU; never fails). */
 ARE_API int32_t are_device_count(void);
+/* Scenes and render workspaces take device memory from a per-device pool
+ * that keeps up to 1 GiB cached after frees, so per-frame scene rebuilds do
+ * not allocate anew.  This returns the cached memory of `device` (-1: every
+ * device the library has used) to the driver; memory in use stays. */
+ARE_API are_status are_trim_memory(int32_t device);
 
 /* Replaces building rt.cpp's Scene (rt.cpp:146-186) / filling an
  * are::ObjectSet: validates the descriptor, builds the SAH BVH on the host,

@@ -126,3 +126,10 @@ def test_scene_churn_reuses_pooled_memory(gpu_lib):
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
+    # the cached blocks go back to the driver on request
+    are.trim_memory(-1)
+    torch.cuda.synchronize()
+    free2, _ = torch.cuda.mem_get_info()
+    assert free2 > free1
+    with pytest.raises(are.AreError):
+        are.trim_memory(1000)
