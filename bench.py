@@ -636,7 +636,8 @@ def main() -> None:
     if mega:
         dom, t_dom, n_launch = "k_tail (megakernel)", tot["other"], args.steps
         algo_bytes = BYTES_MEGA_SAMPLE * samples + BYTES_MEGA_SEGMENT * segments
-        per_sample = traffic.get(f"megakernel_{args.workload}", {}).get("bytes_per_sample")
+        prof = traffic.get(f"megakernel_{args.workload}", {})
+        per_sample = prof.get("bytes_per_sample")
         traffic_launch = round(per_sample * samples / n_launch) if per_sample is not None else None
     else:
         algo = {"intersect": BYTES_INTERSECT * wave_segments,
@@ -651,6 +652,12 @@ def main() -> None:
             "avg_launch_us": round(t_dom * 1e3 / n_launch, 2),
             "kernel_ms": {k: round(v, 2) for k, v in tot.items()},
             "traffic": traffic_launch}
+    if mega:
+        # what actually bounds the megakernel: instruction issue (ncu, profiles/megakernel_*.md); its DRAM
+        # traffic is a small fraction of the wavefront-equivalent bytes above
+        roof["issue_active"] = prof.get("issue_active")
+        roof["note"] = ("megakernel: path state in registers; achieved = wavefront-equivalent algorithmic bytes / "
+                        "launch time; the kernel is issue-bound (issue_active, from ncu)")
 
     # end to end through the C ABI with host buffers
     host_rgb = np.empty(W * H * 3, np.float32)
