@@ -61,7 +61,7 @@ __device__ __forceinline__ bool accumulate(const Wave &W, f3 L, int64_t &item, i
 	if (j >= chunk_len) {
 		// item complete: publish its sums, take the next item
 		W.item_s[item] = make_float4(sm.x - cm.x, sm.y - cm.y, sm.z - cm.z, 0.f);
-		W.item_q[item] = q;
+		if (W.item_q) W.item_q[item] = q;  // one-sample items: q is fl(L L), which resolve recomputes
 		sm = cm = q = make_float4(0.f, 0.f, 0.f, 0.f);
 		item = (int64_t)atomicAdd(next_item, 1u);
 		j = 0;

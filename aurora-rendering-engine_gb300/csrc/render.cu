@@ -302,7 +302,10 @@ __global__ void k_resolve(Wave W, float *__restrict__ rgb, float *__restrict__ v
 		float s[3] = { 0.f, 0.f, 0.f }, c[3] = { 0.f, 0.f, 0.f }, q[3] = { 0.f, 0.f, 0.f };
 		for (int ch = 0; ch < W.nchunk; ++ch) {
 			int64_t it = (int64_t)ch * W.npix + px;
-			float4 a = W.item_s[it], b = W.item_q[it];
+			const float4 a = W.item_s[it];
+			// one-sample items store no square: fl(a a) is the value accumulate computed (fma(L, L, 0))
+			const float4 b = W.item_q ? W.item_q[it]
+									  : make_float4(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y), __fmul_rn(a.z, a.z), 0.f);
 			float v[3] = { a.x, a.y, a.z }, w[3] = { b.x, b.y, b.z };
 			for (int k = 0; k < 3; ++k) {
 				float y = v[k] - c[k];
@@ -431,10 +434,19 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	int P = p.pool_size > 0 ? p.pool_size : mega ? g_tail * BLOCK : (1 << 20);
 	if (P > (1 << 24)) return bad("pool_size too large (max 2^24)");
 	int chunk = p.chunk;
-	// small work items keep the end-of-frame tail short (a slot finishes its item before going idle),
-	// large ones take fewer atomics on the next-item counter
-	if (chunk <= 0)
-		chunk = (int)std::min<int64_t>(16, std::max<int64_t>(1, total / ((mega ? 64 : 16) * (int64_t)P)));
+	// wavefront: small work items keep the end-of-frame tail short (a slot finishes its item before
+	// going idle), large ones take fewer atomics on the next-item counter.  Megakernel: one sample per
+	// item measured fastest on every workload (mesh 967 -> 1201, spheres at 256 spp 1908 -> 2525
+	// Msamples/s against 16-sample items); its items cost 16 bytes each, so larger items only when the
+	// item sums of one-sample items would pass MEGA_ITEM_BUDGET bytes
+	if (chunk <= 0) {
+		if (mega && total * 16 <= MEGA_ITEM_BUDGET)
+			chunk = 1;
+		else if (mega)
+			chunk = (int)std::min<int64_t>(p.spp, (total * 32 + MEGA_ITEM_BUDGET - 1) / MEGA_ITEM_BUDGET);
+		else
+			chunk = (int)std::min<int64_t>(16, std::max<int64_t>(1, total / (16 * (int64_t)P)));
+	}
 	chunk = std::min(chunk, p.spp);
 	W.chunk = chunk;
 	W.nchunk = (p.spp + chunk - 1) / chunk;
@@ -469,7 +481,9 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		if (are_status st = pool_alloc(sc, need, &sc->ws)) return st;
 		sc->ws_bytes = need;
 	}
-	size_t item_need = (size_t)W.n_items * 2 * sizeof(float4) + 2 * (size_t)W.npix * 3 * sizeof(float);
+	const bool one_sample_items = W.chunk == 1;  // no per-item sum of squares (see k_resolve)
+	size_t item_need = (size_t)W.n_items * (one_sample_items ? 1 : 2) * sizeof(float4) +
+		2 * (size_t)W.npix * 3 * sizeof(float);
 	if (item_need > sc->items_bytes) {
 		pool_free(sc, sc->items);
 		sc->items = nullptr;
@@ -487,9 +501,9 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		W.cnt = carve<unsigned>(z, 64);
 		W.stat = carve<unsigned long long>(z, 8);
 		W.item_s = (float4 *)sc->items;
-		W.item_q = W.item_s + W.n_items;
+		W.item_q = one_sample_items ? nullptr : W.item_s + W.n_items;
 	}
-	float *d_rgb = (float *)(W.item_q + W.n_items);
+	float *d_rgb = (float *)(W.item_s + W.n_items * (one_sample_items ? 1 : 2));
 	float *d_var = d_rgb + 3 * (size_t)W.npix;
 	const bool dev_out = (p.flags & ARE_FLAG_DEVICE_OUTPUT) != 0;
 

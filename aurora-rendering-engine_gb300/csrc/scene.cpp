@@ -6,6 +6,7 @@
 // reference's error behaviour where it has one: are::Triangle's constructor
 // rejects null materials/textures, zero edge vectors and collinear edges
 // (src/object/triangle.cpp:9-46); here those become ARE_ERR_INVALID_ARGUMENT.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -22,7 +23,15 @@ namespace are_core {
 
 namespace {
 
-constexpr uint64_t POOL_KEEP_BYTES = 1ull << 30;  // cached in the pool between frees
+// cached in the pool between frees: an eighth of the device's memory (at least 1 GiB), so the
+// one-sample item sums of a large frame (several GB) are reused by the next scene, not mapped anew
+uint64_t pool_keep_bytes(int device) {
+	size_t total = 0;
+	cudaDeviceProp prop{};
+	if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) total = prop.totalGlobalMem;
+	cudaGetLastError();
+	return std::max<uint64_t>(1ull << 30, (uint64_t)total / 8);
+}
 
 std::mutex g_pool_mu;
 cudaMemPool_t g_pools[256];
@@ -53,7 +62,7 @@ are_status pool_alloc(are_scene *sc, size_t bytes, void **p) {
 			props.location.type = cudaMemLocationTypeDevice;
 			props.location.id = sc->device;
 			if (cudaMemPoolCreate(&g_pools[sc->device], &props) == cudaSuccess) {
-				uint64_t keep = POOL_KEEP_BYTES;
+				uint64_t keep = pool_keep_bytes(sc->device);
 				cudaMemPoolSetAttribute(g_pools[sc->device], cudaMemPoolAttrReleaseThreshold, &keep);
 			} else {
 				cudaGetLastError();

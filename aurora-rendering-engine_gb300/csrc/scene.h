@@ -48,7 +48,8 @@ const char *last_error();
 are_status cuda_status(cudaError_t e, const char *what);
 
 // Memory.  Scene arrays and render workspaces come from one stream-ordered
-// pool per device (cudaMemPool) that keeps up to 1 GiB cached after frees, so a
+// pool per device (cudaMemPool) that keeps up to an eighth of the device's
+// memory (at least 1 GiB) cached after frees, so a
 // caller that creates, renders and destroys a scene per frame does not pay
 // cudaMalloc and cudaFree (each a device-wide synchronisation) every time.
 // Allocations are ordered on the scene's stream; pool_free releases on it.

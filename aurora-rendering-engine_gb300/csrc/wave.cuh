@@ -16,6 +16,7 @@ constexpr int BLOCK = 256;
 // linear-scan scenes run best at 4 (64 registers), BVH scenes at 2 (deeper traversal state)
 constexpr int TAIL_MIN_BLOCKS_LINEAR = 4;
 constexpr int TAIL_MIN_BLOCKS_BVH = 2;
+constexpr int64_t MEGA_ITEM_BUDGET = 12ll << 30;  // bytes of per-item sums the megakernel's automatic chunk allows
 constexpr int TAIL_SHORT_STACK = 8;       // binary-tree traversal-stack entries per thread in shared memory
 constexpr int TAIL_SHORT_STACK_WIDE = 8;  // the same for the 4-wide tree
 
@@ -33,7 +34,7 @@ struct Wave {
 	unsigned *cnt;    // [0],[1] queue sizes, [3] next work item, [4] error word, [6], [7] guided counters
 	unsigned long long *stat;  // [0] segments, [1] samples
 	float4 *item_s;   // per work item: sum (xyz)
-	float4 *item_q;   // per work item: sum of squares
+	float4 *item_q;   // per work item: sum of squares; null when every item is one sample (resolve squares the sum)
 	int32_t P;
 	int32_t npix, spp, chunk, nchunk;
 	int64_t n_items;

@@ -201,8 +201,8 @@ ARE_API int32_t are_version(void);
 /* Number of CUDA devices visible (0 when no GPU; never fails). */
 ARE_API int32_t are_device_count(void);
 /* Scenes and render workspaces take device memory from a per-device pool
- * that keeps up to 1 GiB cached after frees, so per-frame scene rebuilds do
- * not allocate anew.  This returns the cached memory of `device` (-1: every
+ * that keeps up to an eighth of the device's memory (at least 1 GiB) cached
+ * after frees, so per-frame scene rebuilds do not allocate anew.  This returns the cached memory of `device` (-1: every
  * device the library has used) to the driver; memory in use stays. */
 ARE_API are_status are_trim_memory(int32_t device);
 
