@@ -166,7 +166,7 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_tail launch");
 	}
-	const int g_int = intersect_grid(linear, sc->n_sms);
+	const int g_int = intersect_grid(linear, sc->dev, sc->n_sms);
 	const int g_sh = blocks_for((const void *)k_shade, sc->n_sms);
 	const int64_t max_rounds = (W.n_items / std::max(1, P) + 2) * (int64_t)p.max_depth * W.chunk / GRAPH_ITERS + 16;
 	for (int64_t round = 0; !st && !mega; ++round) {

@@ -95,10 +95,14 @@ __global__ void __launch_bounds__(BLOCK) k_init(Wave W, int n_first) {
 	}
 }
 
-template <bool LINEAR>
+// LINEAR: the warp-cooperative scan of a tiny scene; else the binary tree, or
+// the 4-wide tree (WIDE), with the top INTERSECT_SHORT_STACK stack entries of
+// each thread in shared memory.
+template <bool LINEAR, bool WIDE = false>
 __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par) {
 	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
 	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
+	__shared__ int4 sstack[LINEAR ? 1 : INTERSECT_SHORT_STACK * BLOCK];
 	int n_snodes = 0;
 	const unsigned n = W.cnt[par];
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -111,8 +115,10 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 	if (linear) {
 		stage_prims(S, snodes);
 		__syncthreads();
+	} else if (WIDE) {
+		stage_nodes4(S, snodes, n_snodes);
 	} else {
-		stage_bvh(S, snodes, n_snodes);
+		stage_nodes(S, snodes, n_snodes);
 	}
 	const float4 *__restrict__ qa = W.qa[par];
 	const float4 *__restrict__ qb = W.qb[par];
@@ -129,7 +135,10 @@ __global__ void __launch_bounds__(BLOCK) k_intersect(DevScene S, Wave W, int par
 			h = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, ld3(r0), ld3(r1), W.t_min, inf, active,
 				scratch[threadIdx.x >> 5]);
 		} else if (active) {
-			h = closest_hit_any(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err);
+			h = WIDE ? closest_hit4<INTERSECT_SHORT_STACK>(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err,
+						   sstack + threadIdx.x)
+					 : closest_hit<INTERSECT_SHORT_STACK>(S, snodes, n_snodes, ld3(r0), ld3(r1), W.t_min, inf, err,
+						   sstack + threadIdx.x);
 		}
 		if (active) W.hit[i] = make_float4(h.t, __int_as_float(h.leaf), h.u, h.v);
 	}
@@ -396,12 +405,16 @@ int tail_grid(bool linear, const DevScene &S, int n_sms) { return grid_for(tail_
 void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par) {
 	if (linear)
 		k_intersect<true><<<grid, BLOCK, 0, s>>>(S, W, par);
+	else if (S.n_nodes4 > 0)
+		k_intersect<false, true><<<grid, BLOCK, 0, s>>>(S, W, par);
 	else
-		k_intersect<false><<<grid, BLOCK, 0, s>>>(S, W, par);
+		k_intersect<false, false><<<grid, BLOCK, 0, s>>>(S, W, par);
 }
 
-int intersect_grid(bool linear, int n_sms) {
-	return grid_for(linear ? (const void *)k_intersect<true> : (const void *)k_intersect<false>, n_sms);
+int intersect_grid(bool linear, const DevScene &S, int n_sms) {
+	const void *fn = linear ? (const void *)k_intersect<true>
+							: S.n_nodes4 > 0 ? (const void *)k_intersect<false, true> : (const void *)k_intersect<false, false>;
+	return grid_for(fn, n_sms);
 }
 
 are_status render(are_scene *sc, const are_camera *cam, const are_render_params *prm, float *rgb, float *var,
@@ -422,7 +435,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	// state stays in registers; no queue records go through memory between bounces)
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
 	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
-	const int g_int = intersect_grid(linear, sc->n_sms);
+	const int g_int = intersect_grid(linear, sc->dev, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
 	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
 

@@ -19,6 +19,7 @@ constexpr int TAIL_MIN_BLOCKS_BVH = 2;
 constexpr int64_t MEGA_ITEM_BUDGET = 12ll << 30;  // bytes of per-item sums the megakernel's automatic chunk allows
 constexpr int TAIL_SHORT_STACK = 8;       // binary-tree traversal-stack entries per thread in shared memory
 constexpr int TAIL_SHORT_STACK_WIDE = 8;  // the same for the 4-wide tree
+constexpr int INTERSECT_SHORT_STACK = 4;  // the wavefront's intersect (keeps 4 blocks of 256 per SM)
 
 struct Wave {
 	// Ray queues: one 64-byte record per queued path segment, SoA over 4 float4:
@@ -59,6 +60,6 @@ void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const
 int tail_grid(bool linear, const DevScene &S, int n_sms);
 // k_intersect (render.cu) for a linear-scan or BVH scene on queue par, and its grid
 void launch_intersect(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, int par);
-int intersect_grid(bool linear, int n_sms);
+int intersect_grid(bool linear, const DevScene &S, int n_sms);
 
 }  // namespace are_core

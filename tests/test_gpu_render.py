@@ -77,7 +77,7 @@ def test_deterministic_across_pool_sizes(gpu_lib):
 
 
 def test_full_size_cornell_properties(gpu_lib):
-    """BASELINE-size Cornell frame at reduced spp: every sample completes,
+    """The full-size Cornell frame (600x600) at reduced spp: every sample completes,
     the image is finite and non-negative, and the mean radiance matches a
     second render with another seed within its standard error."""
     s, cam, par = are.build_config(are.CONFIG_CORNELL)
