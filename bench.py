@@ -73,6 +73,27 @@ def dist_env():
     return rank, world, local
 
 
+# The CUDA device this process renders on and the GPU index nvidia-smi reports
+# for it.  Under torchrun (N > 1) each rank sees only its own GPU
+# (CUDA_VISIBLE_DEVICES narrowed before CUDA starts), so torch and the
+# library — which links its own CUDA runtime — agree on device 0.
+DEVICE = 0
+SMI_INDEX = 0
+
+
+def pin_rank_gpu(world: int, local: int) -> None:
+    global DEVICE, SMI_INDEX
+    if world <= 1:
+        DEVICE = SMI_INDEX = local
+        return
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    ids = [v.strip() for v in vis.split(",") if v.strip()] if vis else []
+    mine = ids[local] if local < len(ids) else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = mine
+    DEVICE = 0
+    SMI_INDEX = int(mine) if mine.isdigit() else local
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -270,8 +291,7 @@ def run_batch(args, rank, world) -> None:
 
     import dataclasses
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(DEVICE)
     wl = are.batch_workload(n_scenes=64, seed=2026)
     arrays = [a for a, _, _ in wl]
     cams = [c for _, c, _ in wl]
@@ -291,7 +311,7 @@ def run_batch(args, rank, world) -> None:
     barrier(world)
     torch.cuda.synchronize()
     stats, scene_ms = [], []
-    with ClockSampler(local) as clk:
+    with ClockSampler(SMI_INDEX) as clk:
         for i in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -357,8 +377,7 @@ def run_guided(args, rank, world) -> None:
 
     import are_gb300 as are
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(DEVICE)
     cfg_id, workload = WORKLOADS["guided"]
     scene_arrays, cam, par = are.build_config(cfg_id)
     spp = args.spp if args.spp > 0 else par["spp"]
@@ -374,7 +393,7 @@ def run_guided(args, rank, world) -> None:
     barrier(world)
     torch.cuda.synchronize()
     stats = []
-    with ClockSampler(local) as clk:
+    with ClockSampler(SMI_INDEX) as clk:
         for i in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -439,8 +458,7 @@ def run_legacy(args, rank, world) -> None:
 
     import are_gb300 as are
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(DEVICE)
     scene_arrays, cam, par = are.build_config(are.CONFIG_LEGACY_RT)
     W, H = par["width"], par["height"]
     sc = are.Scene(scene_arrays)
@@ -453,7 +471,7 @@ def run_legacy(args, rank, world) -> None:
     barrier(world)
     torch.cuda.synchronize()
     stats = []
-    with ClockSampler(local) as clk:
+    with ClockSampler(SMI_INDEX) as clk:
         for i in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -559,6 +577,7 @@ def main() -> None:
                     help="where scenes build their BVH: host binned SAH or the device LBVH")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    pin_rank_gpu(world, local)  # before anything starts CUDA
     pg = None
     if world > 1:
         import torch.distributed as dist
@@ -583,7 +602,7 @@ def main() -> None:
 
     import are_gb300 as are
 
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(DEVICE)
     L = are.load()
     cfg_id, workload = WORKLOADS[args.workload]
     scene_arrays, cam, par = are.build_config(cfg_id)
@@ -610,7 +629,7 @@ def main() -> None:
     torch.cuda.synchronize()
     stats = []
     wall0 = time.perf_counter()
-    with ClockSampler(local) as clk:
+    with ClockSampler(SMI_INDEX) as clk:
         for i in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()

@@ -63,3 +63,23 @@ def test_reference_arm_under_torchrun_prints_one_line():
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_rank_gpu_pinning(monkeypatch):
+    """Under torchrun each rank narrows CUDA_VISIBLE_DEVICES to its own GPU
+    before CUDA starts (the library links its own CUDA runtime, so device 0
+    must be the rank's GPU for both it and torch); nvidia-smi keeps the
+    physical index.  One process (N = 1) changes nothing."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", REPO / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "3,5")
+    bench.pin_rank_gpu(2, 1)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "5" and bench.DEVICE == 0 and bench.SMI_INDEX == 5
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    bench.pin_rank_gpu(4, 2)
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "2" and bench.DEVICE == 0 and bench.SMI_INDEX == 2
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    bench.pin_rank_gpu(1, 0)
+    assert "CUDA_VISIBLE_DEVICES" not in os.environ and bench.DEVICE == 0
