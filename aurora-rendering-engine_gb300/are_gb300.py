@@ -25,6 +25,7 @@ LIB_PATH = HERE / "_build" / "libaurora_gb300.so"
 
 MAT_LAMBERTIAN, MAT_METAL, MAT_DIELECTRIC, MAT_DIFFUSE_LIGHT = 0, 1, 2, 3
 TEX_SOLID, TEX_CHECKER, TEX_IMAGE = 0, 1, 2
+FILTER_NEAREST, FILTER_BILINEAR = 0, 1
 MAP_SURFACE_UV, MAP_SPHERICAL = 0, 1
 BG_CONSTANT, BG_SKY_GRADIENT = 0, 1
 TRI_REFERENCE_MT, TRI_WATERTIGHT = 0, 1
@@ -40,7 +41,7 @@ MATERIAL_DTYPE = np.dtype([("type", "<i4"), ("texture", "<i4"), ("fuzz", "<f4"),
                            ("emit", "<f4", 3), ("reflect_ratio", "<f4"), ("tint", "<f4", 3), ("pad_", "<f4")])
 TEXTURE_DTYPE = np.dtype([("type", "<i4"), ("mapping", "<i4"), ("scale", "<f4"), ("width", "<i4"),
                           ("height", "<i4"), ("texel_offset", "<i4"), ("a", "<f4", 3), ("b", "<f4", 3),
-                          ("center", "<f4", 3), ("pad_", "<f4")])
+                          ("center", "<f4", 3), ("filter", "<i4")])
 assert MATERIAL_DTYPE.itemsize == 48 and TEXTURE_DTYPE.itemsize == 64
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "no device",
@@ -83,9 +84,9 @@ class SceneArrays:
 
     # builders -------------------------------------------------------------
     def texture(self, type=TEX_SOLID, a=(0, 0, 0), b=(0, 0, 0), scale=1.0, mapping=MAP_SURFACE_UV,
-                center=(0, 0, 0), width=0, height=0, texel_offset=0) -> int:
+                center=(0, 0, 0), width=0, height=0, texel_offset=0, filter=FILTER_NEAREST) -> int:
         t = np.zeros(1, TEXTURE_DTYPE)
-        t["type"], t["mapping"], t["scale"] = type, mapping, scale
+        t["type"], t["mapping"], t["scale"], t["filter"] = type, mapping, scale, filter
         t["width"], t["height"], t["texel_offset"] = width, height, texel_offset
         t["a"], t["b"], t["center"] = a, b, center
         self.textures = np.concatenate([self.textures, t])

@@ -60,7 +60,7 @@ struct DevTexture {  // mirrors are_texture (64 B)
 	float scale;
 	int32_t width, height, texel_offset;
 	float a[3], b[3], center[3];
-	float pad_;
+	int32_t filter;
 };
 
 struct DevScene {

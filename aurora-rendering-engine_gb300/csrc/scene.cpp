@@ -200,6 +200,8 @@ are_status validate(const are_scene_desc *d) {
 			if (t.width <= 0 || t.height <= 0) return invalid("texture " + std::to_string(i) + ": width and height must be positive");
 			if (t.texel_offset < 0 || (int64_t)t.texel_offset + (int64_t)t.width * t.height > d->n_texels)
 				return invalid("texture " + std::to_string(i) + ": texel range outside texels[]");
+			if (t.filter != ARE_FILTER_NEAREST && t.filter != ARE_FILTER_BILINEAR)
+				return invalid("texture " + std::to_string(i) + ": unknown filter");
 		}
 	}
 	for (int32_t i = 0; i < d->n_materials; ++i) {

@@ -90,9 +90,28 @@ __device__ __forceinline__ f3 tex_eval(const DevScene &S, int ti, float u, float
 	if (t.type == 2) {
 		float fu = u > 0.f ? (u < 1.f ? u : 1.f) : 0.f;
 		float fv = v > 0.f ? (v < 1.f ? v : 1.f) : 0.f;
+		const float *tex = S.texels + 3 * (size_t)t.texel_offset;
+		if (t.filter == 1) {
+			// src/texture.cpp:310-330's bilinear weights, each operation rounded as the oracle's
+			float x = __fsub_rn(__fmul_rn(fu, (float)t.width), 0.5f), y = __fsub_rn(__fmul_rn(__fsub_rn(1.0f, fv), (float)t.height), 0.5f);
+			x = fminf(fmaxf(x, 0.0f), (float)(t.width - 1));
+			y = fminf(fmaxf(y, 0.0f), (float)(t.height - 1));
+			const int ix = (int)floorf(x), iy = (int)floorf(y);
+			const int ix1 = min(ix + 1, t.width - 1), iy1 = min(iy + 1, t.height - 1);
+			const float tx = __fsub_rn(x, (float)ix), ty = __fsub_rn(y, (float)iy);
+			const float sx = __fsub_rn(1.0f, tx), sy = __fsub_rn(1.0f, ty);
+			const float w00 = __fmul_rn(sx, sy), w10 = __fmul_rn(tx, sy), w01 = __fmul_rn(sx, ty), w11 = __fmul_rn(tx, ty);
+			const float *c00 = tex + 3 * ((size_t)iy * t.width + ix), *c10 = tex + 3 * ((size_t)iy * t.width + ix1);
+			const float *c01 = tex + 3 * ((size_t)iy1 * t.width + ix), *c11 = tex + 3 * ((size_t)iy1 * t.width + ix1);
+			float r[3];
+			for (int k = 0; k < 3; ++k)
+				r[k] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(c00[k], w00), __fmul_rn(c10[k], w10)), __fmul_rn(c01[k], w01)),
+					__fmul_rn(c11[k], w11));
+			return f3{ r[0], r[1], r[2] };
+		}
 		int x = min((int)(fu * (float)t.width), t.width - 1);
 		int y = min((int)((1.0f - fv) * (float)t.height), t.height - 1);
-		return ldf3(S.texels + 3 * ((size_t)t.texel_offset + (size_t)y * t.width + x));
+		return ldf3(tex + 3 * ((size_t)y * t.width + x));
 	}
 	return ldf3(t.a);
 }

@@ -86,8 +86,12 @@ typedef struct are_texture {
 	float a[3];              /* SOLID colour / CHECKER even cells */
 	float b[3];              /* CHECKER odd cells */
 	float center[3];         /* SPHERICAL mapping: centre of the sphere */
-	float pad_;
+	int32_t filter;          /* IMAGE: ARE_FILTER_NEAREST (Texture::pixel, src/texture.cpp:77-83) or
+	                            ARE_FILTER_BILINEAR (the weights of src/texture.cpp:310-330; texel centres
+	                            at i + 1/2, coordinates clamped to the grid) */
 } are_texture;
+
+enum { ARE_FILTER_NEAREST = 0, ARE_FILTER_BILINEAR = 1 };
 
 typedef struct are_scene_desc {
 	int32_t n_spheres;

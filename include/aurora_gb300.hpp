@@ -79,9 +79,11 @@ public:
 		return push_texture(t);
 	}
 	// width x height RGB texels, row-major from the top (are::Texture::pixel(x, y))
-	int image(int width, int height, const float *rgb) {
+	// texels row-major from the top, as are::Texture::pixel(x, y); filter ARE_FILTER_NEAREST or _BILINEAR
+	int image(int width, int height, const float *rgb, int filter = ARE_FILTER_NEAREST) {
 		are_texture t{};
 		t.type = ARE_TEX_IMAGE;
+		t.filter = filter;
 		t.width = width, t.height = height;
 		t.texel_offset = (int32_t)(texels_.size() / 3);
 		texels_.insert(texels_.end(), rgb, rgb + (size_t)width * height * 3);

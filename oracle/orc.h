@@ -51,7 +51,7 @@ typedef struct orc_texture {
 	float a[3];
 	float b[3];
 	float center[3];
-	float pad_;
+	int32_t filter; /* image: 0 nearest, 1 bilinear */
 } orc_texture;
 
 typedef struct orc_scene {

@@ -133,3 +133,36 @@ def test_scene_churn_reuses_pooled_memory(gpu_lib):
     assert free2 > free1
     with pytest.raises(are.AreError):
         are.trim_memory(1000)
+
+
+def textured_quad(filt):
+    """A 5x4 random image texture on a lambertian quad under a constant white
+    sky: with roulette off and two segments per path, a pixel's radiance is
+    exactly the texture at its camera ray's hit (albedo x sky)."""
+    rng = np.random.Generator(np.random.PCG64(9))
+    s = are.SceneArrays()
+    s.bg_a = (1.0, 1.0, 1.0)
+    s.texels = rng.uniform(0.0, 1.0, (5 * 4, 3)).astype(np.float32)
+    t = s.texture(are.TEX_IMAGE, width=5, height=4, texel_offset=0, filter=filt)
+    s.add_quads([-1, -1, 0, 2, 0, 0, 0, 2, 0], s.material(are.MAT_LAMBERTIAN, texture=t))
+    cam = dict(lookfrom=(0, 0, 3), lookat=(0, 0, 0), vup=(0, 1, 0), vfov_deg=40.0, aperture=0.0, focus_dist=3.0)
+    par = dict(width=48, height=48, spp=1, max_depth=2, seed=1, rr_depth=-1, t_min=1e-4,
+               flags=are.FLAG_NO_JITTER, chunk=1)
+    return s, cam, par
+
+
+def test_image_texture_filters(gpu_lib, oracle, nthreads):
+    """Nearest (are::Texture::pixel) and bilinear (src/texture.cpp:310-330's
+    weights) texel lookups: the GPU's image equals the oracle's, and the two
+    filters give different images."""
+    out = {}
+    for filt in (are.FILTER_NEAREST, are.FILTER_BILINEAR):
+        s, cam, par = textured_quad(filt)
+        img, _, st = render_both(are.Scene(s), cam, par)
+        ref, _, _ = oracle.render(oracle.prepare(s), cam, par, nthreads=nthreads)
+        assert st["error_word"] == 0
+        assert np.allclose(img, ref, rtol=1e-5, atol=1e-6), np.abs(img - ref).max()
+        out[filt] = img
+    hit = out[are.FILTER_NEAREST] < 0.999  # pixels on the quad (the sky is exactly 1)
+    assert hit.mean() > 0.3
+    assert not np.allclose(out[are.FILTER_NEAREST][hit], out[are.FILTER_BILINEAR][hit], atol=1e-3)
