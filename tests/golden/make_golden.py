@@ -11,6 +11,8 @@ oracle/_ref/, and this script records their outputs on seeded inputs:
 * lib_kat.npz         are::reflect / are::refract, are::Plane::intersect_ray,
                       are::Triangle FP64 intersect_ray and constructor checks
 * rt_render.npz       rt.cpp render() with std::random_device fixed to a seed
+* rt_out_diffuse.npz  32x32-pixel block means of experiments/out_diffuse.ppm, the
+                      reference's own committed rt.cpp render (512x512, unknown seed)
 
 Usage: python tests/golden/make_golden.py   (from the repository root)
 """
@@ -39,8 +41,21 @@ def dp(a):
     return a.ctypes.data_as(_d)
 
 
+def out_diffuse_summary() -> None:
+    """Block means of the reference's committed render (a P6 PPM, rt.cpp:377-392);
+    its seed is unknown (rt.cpp:348-351), so only statistics can be compared."""
+    raw = (obuild.REF_ROOT / "experiments" / "out_diffuse.ppm").read_bytes()
+    magic, size, maxval, body = raw.split(b"\n", 3)
+    w, h = map(int, size.split())
+    assert magic == b"P6" and maxval == b"255" and len(body) == w * h * 3
+    img = np.frombuffer(body, np.uint8).reshape(h, w, 3).astype(np.float64)
+    blocks = img.reshape(h // 32, 32, w // 32, 32, 3).mean((1, 3))
+    np.savez_compressed(HERE / "rt_out_diffuse.npz", width=w, height=h, block=32, means=blocks)
+
+
 def main() -> None:
     obuild.build_ref()
+    out_diffuse_summary()
     ref = RefRT()
     lib = RefLib()
 

@@ -191,3 +191,17 @@ def test_reference_estimator_full_frame_bitexact(oracle):
     s, cam, par = are.build_config(are.CONFIG_LEGACY_RT)
     img = render_legacy(oracle, oracle.prepare(s, accel=0), cam, par, rng_mode=1, mt_seed=3)
     assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+
+
+def test_oracle_estimator_matches_the_references_committed_render(oracle):
+    """The oracle's restatement of rt.cpp's estimator against
+    experiments/out_diffuse.ppm, the reference's own committed render (its
+    seed unknown, so 32x32-pixel block means within 1.5 levels)."""
+    from oracle.orc import render_legacy
+    g = np.load(GOLDEN / "rt_out_diffuse.npz")
+    s, cam, par = are.build_config(are.CONFIG_LEGACY_RT)
+    img = render_legacy(oracle, oracle.prepare(s, accel=0), cam, par, rng_mode=1, mt_seed=11)
+    q = oracle.quantize(img, 0, 2.2).reshape(int(g["height"]), int(g["width"]), 3).astype(np.float64)
+    b = int(g["block"])
+    d = np.abs(q.reshape(q.shape[0] // b, b, q.shape[1] // b, b, 3).mean((1, 3)) - g["means"])
+    assert d.max() < 1.5 and d.mean() < 0.2, (d.max(), d.mean())
