@@ -61,7 +61,7 @@ struct Builder {
 			fn(first, first + count, 0);
 			return 1;
 		}
-		static const int hw = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+		static const int hw = (int)hw_threads();
 		const int nc = std::min(hw, (int)(count / (PAR_RANGE / 4)));
 		if (nc <= 1) {
 			fn(first, first + count, 0);
@@ -275,8 +275,8 @@ struct Builder {
 		// par_min primitives are set aside and built by worker threads, each into
 		// its own node list, then appended.  Every split depends only on the
 		// subtree's own primitives, so the tree is the one a single thread builds.
-		static const int hw_threads = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-		const int32_t par_min = std::max<int32_t>(4096, n / (4 * hw_threads));
+		static const int n_hw = (int)hw_threads();
+		const int32_t par_min = std::max<int32_t>(4096, n / (4 * n_hw));
 		std::vector<Job> deferred;
 		std::vector<Job> level{ { 0, 0, n, 0 } };
 		nodes.push_back(TmpNode{});
@@ -292,7 +292,7 @@ struct Builder {
 				t.depth = j.depth;
 				mids[k] = split(j.first, j.count, j.depth, lo, hi, clo, chi);
 			};
-			if ((int)level.size() >= hw_threads) {
+			if ((int)level.size() >= n_hw) {
 				std::atomic<size_t> next{ 0 };
 				auto worker = [&]() {
 					inline_passes() = true;
@@ -300,7 +300,7 @@ struct Builder {
 					inline_passes() = false;
 				};
 				std::vector<std::thread> pool;
-				for (int t = 1; t < hw_threads; ++t) pool.emplace_back(worker);
+				for (int t = 1; t < n_hw; ++t) pool.emplace_back(worker);
 				worker();
 				for (std::thread &t : pool) t.join();
 			} else {
@@ -351,27 +351,34 @@ struct Builder {
 			}
 			inline_passes() = false;
 		};
-		const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-		const unsigned nthreads = (unsigned)std::min<size_t>(hw, deferred.size());
+		const unsigned nthreads = (unsigned)std::min<size_t>(hw_threads(), deferred.size());
 		std::vector<std::thread> pool;
 		for (unsigned t = 1; t < nthreads; ++t) pool.emplace_back(worker);
 		worker();
 		for (std::thread &t : pool) t.join();
-		// append each subtree: local node 0 fills the placeholder, the rest shift by base - 1
+		// append each subtree (in job order, copied in parallel): local node 0
+		// fills the placeholder, the rest shift by base - 1
+		std::vector<int32_t> base(deferred.size());
+		size_t total = nodes.size();
 		for (size_t k = 0; k < deferred.size(); ++k) {
+			base[k] = (int32_t)total;
+			total += local[k].size() - 1;
+			max_depth = std::max(max_depth, local_depth[k]);
+		}
+		nodes.resize(total);
+		run_jobs(deferred.size(), nthreads, [&](size_t k) {
 			const std::vector<TmpNode> &ln = local[k];
-			const int32_t base = (int32_t)nodes.size();
-			auto map = [&](int32_t i) { return i < 0 ? i : base + i - 1; };
+			const int32_t b0 = base[k];
+			auto map = [&](int32_t i) { return i < 0 ? i : b0 + i - 1; };
 			TmpNode root = ln[0];
 			root.left = map(root.left), root.right = map(root.right);
 			nodes[deferred[k].node] = root;
 			for (size_t i = 1; i < ln.size(); ++i) {
 				TmpNode t = ln[i];
 				t.left = map(t.left), t.right = map(t.right);
-				nodes.push_back(t);
+				nodes[(size_t)b0 + i - 1] = t;
 			}
-			max_depth = std::max(max_depth, local_depth[k]);
-		}
+		});
 	}
 
 	// one step of the build: bounds and split of job j's range into node j.node of `ns`
@@ -424,20 +431,15 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 	// layout: root at 0, padding at 1, sibling pairs at even indices; pairs are
 	// allocated breadth-first until 1024 nodes exist, depth-first afterwards.
 	const size_t ntmp = b.nodes.size();
+	const unsigned nthreads = ntmp < ((size_t)1 << 16) ? 1u : hw_threads();
 	std::vector<int32_t> slot(ntmp, -1);
 	slot[0] = 0;
 	int32_t next = 2;
 	std::deque<int32_t> work;
 	work.push_back(0);
-	while (!work.empty()) {
-		int32_t t;
-		if (next < SMEM_NODES) {
-			t = work.front();
-			work.pop_front();
-		} else {
-			t = work.back();
-			work.pop_back();
-		}
+	while (!work.empty() && next < SMEM_NODES) {
+		const int32_t t = work.front();
+		work.pop_front();
 		const TmpNode &tn = b.nodes[t];
 		if (tn.left < 0) continue;
 		slot[tn.left] = next;
@@ -446,11 +448,42 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 		if (next < SMEM_NODES) {
 			work.push_back(tn.left);
 			work.push_back(tn.right);
-		} else {  // depth-first: visit the left child next
+		} else {  // depth-first from here: the left child first
 			work.push_back(tn.right);
 			work.push_back(tn.left);
 		}
 	}
+	// Depth-first, the queued subtrees are laid out one after another, last
+	// queued first, each over a contiguous run of slots as long as its node
+	// count less one; so each is laid out on its own, in parallel.  Children
+	// always follow their parent in the build's list, so one backward pass
+	// counts every subtree's nodes.
+	std::vector<std::pair<int32_t, int32_t>> dfs;  // (subtree root, first slot of its descendants)
+	if (!work.empty()) {
+		std::vector<int32_t> sub(ntmp, 1);
+		for (size_t t = ntmp; t-- > 0;) {
+			const TmpNode &tn = b.nodes[t];
+			if (tn.left >= 0) sub[t] = 1 + sub[tn.left] + sub[tn.right];
+		}
+		for (; !work.empty(); work.pop_back()) {
+			dfs.push_back({ work.back(), next });
+			next += sub[work.back()] - 1;
+		}
+	}
+	run_jobs(dfs.size(), nthreads, [&](size_t k) {
+		std::vector<int32_t> st{ dfs[k].first };
+		int32_t nx = dfs[k].second;
+		while (!st.empty()) {
+			const TmpNode &tn = b.nodes[st.back()];
+			st.pop_back();
+			if (tn.left < 0) continue;
+			slot[tn.left] = nx;
+			slot[tn.right] = nx + 1;
+			nx += 2;
+			st.push_back(tn.right);
+			st.push_back(tn.left);
+		}
+	});
 	r.n_nodes = next;
 	r.nodes.assign(8 * (size_t)next, 0.0f);
 	// padding node 1: inverted box, never hit
@@ -459,8 +492,6 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 	// leaves keep the primitive ranges of the build order; node records are
 	// written in parallel ranges (each node independently)
 	r.order = b.idx;
-	const unsigned nthreads =
-		ntmp < ((size_t)1 << 16) ? 1u : std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
 	std::vector<int32_t> part_max_leaf(nthreads, 0);
 	auto write_range = [&](unsigned part) {
 		int32_t &max_leaf = part_max_leaf[part];
@@ -546,60 +577,110 @@ std::vector<float> collapse_bvh4(const BvhResult &bvh, int bfs_nodes) {
 	refs.push_back({ -1, -1, -1, -1 });
 	kids_of.push_back({ -1, -1, -1, -1 });
 	nkids.push_back(0);
-	while (!work.empty()) {
-		int32_t w;
-		if ((int)src.size() < bfs_nodes) {
-			w = work.front();
-			work.pop_front();
-		} else {
-			w = work.back();
-			work.pop_back();
-		}
+	// wide node w: its children (records) and the numbers of its interior children,
+	// taken from next_index(binary record) in child order
+	auto expand = [&](int32_t w, auto &&next_index, int32_t inner[4]) {
 		int32_t kids[4];
 		const int n = gather(src[w], kids);
 		nkids[w] = n;
-		int32_t inner[4];
 		int n_inner = 0;
 		for (int k = 0; k < n; ++k) {
 			kids_of[w][k] = kids[k];
 			if (is_leaf(kids[k])) continue;
-			const int32_t m = (int32_t)src.size();
-			src.push_back(kids[k]);
-			refs.push_back({ -1, -1, -1, -1 });
-			kids_of.push_back({ -1, -1, -1, -1 });
-			nkids.push_back(0);
+			const int32_t m = next_index(kids[k]);
 			refs[w][k] = m;
 			inner[n_inner++] = m;
 		}
+		return n_inner;
+	};
+	auto append = [&](int32_t r) {
+		src.push_back(r);
+		refs.push_back({ -1, -1, -1, -1 });
+		kids_of.push_back({ -1, -1, -1, -1 });
+		nkids.push_back(0);
+		return (int32_t)src.size() - 1;
+	};
+	while (!work.empty() && (int)src.size() < bfs_nodes) {
+		const int32_t w = work.front();
+		work.pop_front();
+		int32_t inner[4];
+		const int n_inner = expand(w, append, inner);
 		if ((int)src.size() < bfs_nodes) {
 			for (int k = 0; k < n_inner; ++k) work.push_back(inner[k]);
-		} else {  // depth-first: the first child next
+		} else {  // depth-first from here: the first child next
 			for (int k = n_inner - 1; k >= 0; --k) work.push_back(inner[k]);
 		}
 	}
+	// Depth-first, the queued wide nodes' subtrees are numbered one after
+	// another, last queued first, each over a contiguous run as long as its
+	// count of wide descendants: one parallel pass counts them, a second
+	// numbers and fills each subtree on its own.
+	const unsigned nthreads = bvh.n_nodes < (1 << 16) ? 1u : hw_threads();
+	std::vector<int32_t> roots(work.rbegin(), work.rend());
+	std::vector<int32_t> first(roots.size());
+	run_jobs(roots.size(), nthreads, [&](size_t k) {
+		std::vector<int32_t> st{ src[roots[k]] };
+		int32_t c = 0;
+		while (!st.empty()) {
+			int32_t kids[4];
+			const int n = gather(st.back(), kids);
+			st.pop_back();
+			for (int i = 0; i < n; ++i)
+				if (!is_leaf(kids[i])) ++c, st.push_back(kids[i]);
+		}
+		first[k] = c;
+	});
+	size_t total = src.size();
+	for (int32_t &f : first) {
+		const int32_t c = f;
+		f = (int32_t)total;
+		total += c;
+	}
+	src.resize(total);
+	refs.resize(total, { -1, -1, -1, -1 });
+	kids_of.resize(total, { -1, -1, -1, -1 });
+	nkids.resize(total, 0);
+	run_jobs(roots.size(), nthreads, [&](size_t k) {
+		std::vector<int32_t> st{ roots[k] };
+		int32_t nx = first[k];
+		auto take = [&](int32_t r) {
+			src[nx] = r;
+			return nx++;
+		};
+		while (!st.empty()) {
+			const int32_t w = st.back();
+			st.pop_back();
+			int32_t inner[4];
+			const int n_inner = expand(w, take, inner);
+			for (int i = n_inner - 1; i >= 0; --i) st.push_back(inner[i]);
+		}
+	});
 	const size_t nw = src.size();
 	out.assign(32 * nw, 0.0f);
-	for (size_t w = 0; w < nw; ++w) {
-		for (int k = 0; k < 4; ++k) {
-			float *o = &out[32 * w + 8 * (size_t)k];
-			if (k >= nkids[w]) {
-				// unused slot: an empty leaf (count -1, no primitives), so entering it does nothing
-				// (a min > max box is no guard: the slab test orders each axis's two planes)
-				const int32_t a = 0, b = -1;
-				for (int j = 0; j < 3; ++j) o[j] = 1.0f, o[4 + j] = -1.0f;
-				std::memcpy(&o[3], &a, 4);
-				std::memcpy(&o[7], &b, 4);
-				continue;
-			}
-			const int32_t r = kids_of[w][k];
-			std::memcpy(o, &rec[8 * (size_t)r], 32);  // box, first / count as in the binary record
-			if (!is_leaf(r)) {
-				const int32_t a = refs[w][k], b = 0;
-				std::memcpy(&o[3], &a, 4);
-				std::memcpy(&o[7], &b, 4);
+	const size_t nparts = nthreads > 1 ? 4 * (size_t)nthreads : 1;
+	run_jobs(nparts, nthreads, [&](size_t part) {
+		for (size_t w = nw * part / nparts; w < nw * (part + 1) / nparts; ++w) {
+			for (int k = 0; k < 4; ++k) {
+				float *o = &out[32 * w + 8 * (size_t)k];
+				if (k >= nkids[w]) {
+					// unused slot: an empty leaf (count -1, no primitives), so entering it does nothing
+					// (a min > max box is no guard: the slab test orders each axis's two planes)
+					const int32_t a = 0, b = -1;
+					for (int j = 0; j < 3; ++j) o[j] = 1.0f, o[4 + j] = -1.0f;
+					std::memcpy(&o[3], &a, 4);
+					std::memcpy(&o[7], &b, 4);
+					continue;
+				}
+				const int32_t r = kids_of[w][k];
+				std::memcpy(o, &rec[8 * (size_t)r], 32);  // box, first / count as in the binary record
+				if (!is_leaf(r)) {
+					const int32_t a = refs[w][k], b = 0;
+					std::memcpy(&o[3], &a, 4);
+					std::memcpy(&o[7], &b, 4);
+				}
 			}
 		}
-	}
+	});
 	return out;
 }
 

@@ -5,10 +5,42 @@
 // on equal t).
 #pragma once
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <thread>
 #include <vector>
 
 namespace are_core {
+
+// host threads for the scene build (at most 32)
+inline unsigned hw_threads() { return std::max(1u, std::min(32u, std::thread::hardware_concurrency())); }
+
+// fn(k) for every k in [0, n), whole jobs taken in turn by up to `threads` threads
+template <class F>
+void run_jobs(size_t n, unsigned threads, F fn) {
+	threads = (unsigned)std::min<size_t>(threads, n);
+	if (threads <= 1) {
+		for (size_t k = 0; k < n; ++k) fn(k);
+		return;
+	}
+	std::atomic<size_t> next{ 0 };
+	auto worker = [&]() {
+		for (size_t k; (k = next.fetch_add(1)) < n;) fn(k);
+	};
+	std::vector<std::thread> pool;
+	for (unsigned t = 1; t < threads; ++t) pool.emplace_back(worker);
+	worker();
+	for (std::thread &t : pool) t.join();
+}
+
+// fn(begin, end) over [0, n) in contiguous parts, on several threads once n reaches 2^16
+template <class F>
+void parallel_ranges(size_t n, F fn) {
+	const unsigned threads = n < ((size_t)1 << 16) ? 1u : hw_threads();
+	const size_t parts = threads > 1 ? 4 * (size_t)threads : 1;
+	run_jobs(parts, threads, [&](size_t p) { fn(n * p / parts, n * (p + 1) / parts); });
+}
 
 struct PrimBox {
 	double lo[3], hi[3];

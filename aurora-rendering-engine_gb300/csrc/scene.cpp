@@ -7,6 +7,7 @@
 // rejects null materials/textures, zero edge vectors and collinear edges
 // (src/object/triangle.cpp:9-46); here those become ARE_ERR_INVALID_ARGUMENT.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -232,7 +233,7 @@ are_status validate(const are_scene_desc *d) {
 		if (near_zero(u) || near_zero(v) || near_zero(c)) return invalid("quad " + std::to_string(i) + ": degenerate edges");
 		if (are_status st = check_mat(d->quad_mat[i], "quad", i)) return st;
 	}
-	for (int32_t i = 0; i < d->n_triangles; ++i) {
+	auto check_tri = [&](int32_t i) -> are_status {
 		const float *t = d->triangles + 9 * (size_t)i;
 		if (!finite3(t) || !finite3(t + 3) || !finite3(t + 6))
 			return invalid("triangle " + std::to_string(i) + ": non-finite vertex");
@@ -242,9 +243,19 @@ are_status validate(const are_scene_desc *d) {
 		// src/object/triangle.cpp:21-36: zero or collinear edge vectors throw
 		if (near_zero(u) || near_zero(v)) return invalid("triangle " + std::to_string(i) + ": edge vector is zero");
 		if (near_zero(c)) return invalid("triangle " + std::to_string(i) + ": edge vectors are collinear");
-		if (are_status st = check_mat(d->triangle_mat[i], "triangle", i)) return st;
-	}
-	return ARE_OK;
+		return check_mat(d->triangle_mat[i], "triangle", i);
+	};
+	// the lowest-numbered bad triangle, searched in parallel, is the one reported (on this thread)
+	std::atomic<int32_t> first_bad{ d->n_triangles };
+	parallel_ranges((size_t)d->n_triangles, [&](size_t i0, size_t i1) {
+		for (size_t i = i0; i < i1 && (int32_t)i < first_bad.load(std::memory_order_relaxed); ++i)
+			if (check_tri((int32_t)i) != ARE_OK) {
+				int32_t cur = first_bad.load();
+				while ((int32_t)i < cur && !first_bad.compare_exchange_weak(cur, (int32_t)i)) {}
+				break;
+			}
+	});
+	return first_bad < d->n_triangles ? check_tri(first_bad) : ARE_OK;
 }
 
 template <class T>
@@ -378,27 +389,28 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 
 	// primitive bounds in double
 	std::vector<PrimBox> boxes((size_t)n);
-	for (int32_t i = 0; i < ns; ++i) {
-		const float *s = d->spheres + 4 * (size_t)i;
-		for (int k = 0; k < 3; ++k) boxes[i].lo[k] = (double)s[k] - s[3], boxes[i].hi[k] = (double)s[k] + s[3];
-	}
-	for (int32_t i = 0; i < nq; ++i) {
-		const float *q = d->quads + 9 * (size_t)i;
-		PrimBox &b = boxes[ns + i];
-		for (int k = 0; k < 3; ++k) {
-			double c0 = q[k], c1 = (double)q[k] + q[3 + k], c2 = (double)q[k] + q[6 + k], c3 = c1 + q[6 + k];
-			b.lo[k] = std::fmin(std::fmin(c0, c1), std::fmin(c2, c3));
-			b.hi[k] = std::fmax(std::fmax(c0, c1), std::fmax(c2, c3));
+	parallel_ranges((size_t)n, [&](size_t i0, size_t i1) {
+		for (size_t i = i0; i < i1; ++i) {
+			PrimBox &b = boxes[i];
+			if (i < (size_t)ns) {
+				const float *s = d->spheres + 4 * i;
+				for (int k = 0; k < 3; ++k) b.lo[k] = (double)s[k] - s[3], b.hi[k] = (double)s[k] + s[3];
+			} else if (i < (size_t)(ns + nq)) {
+				const float *q = d->quads + 9 * (i - ns);
+				for (int k = 0; k < 3; ++k) {
+					double c0 = q[k], c1 = (double)q[k] + q[3 + k], c2 = (double)q[k] + q[6 + k], c3 = c1 + q[6 + k];
+					b.lo[k] = std::fmin(std::fmin(c0, c1), std::fmin(c2, c3));
+					b.hi[k] = std::fmax(std::fmax(c0, c1), std::fmax(c2, c3));
+				}
+			} else {
+				const float *t = d->triangles + 9 * (i - ns - nq);
+				for (int k = 0; k < 3; ++k) {
+					b.lo[k] = std::fmin(std::fmin((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
+					b.hi[k] = std::fmax(std::fmax((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
+				}
+			}
 		}
-	}
-	for (int32_t i = 0; i < nt; ++i) {
-		const float *t = d->triangles + 9 * (size_t)i;
-		PrimBox &b = boxes[ns + nq + i];
-		for (int k = 0; k < 3; ++k) {
-			b.lo[k] = std::fmin(std::fmin((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
-			b.hi[k] = std::fmax(std::fmax((double)t[k], (double)t[3 + k]), (double)t[6 + k]);
-		}
-	}
+	});
 	BvhResult bvh = build_bvh(boxes, d->bvh_leaf_size);
 
 	// SoA records in leaf order
@@ -406,26 +418,28 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	std::vector<int32_t> gid((size_t)std::max(n, 1), 0), mat((size_t)std::max(n, 1), 0);
 	std::vector<float> tri_uv;
 	if (d->triangle_uv && nt) tri_uv.assign(6 * (size_t)n, 0.0f);
-	for (int32_t j = 0; j < n; ++j) {
-		int32_t g = bvh.order[j];
-		float *o = &prims[12 * (size_t)j];
-		gid[j] = g;
-		if (g < ns) {
-			std::memcpy(o, d->spheres + 4 * (size_t)g, 16);
-			mat[j] = d->sphere_mat[g];
-		} else if (g < ns + nq) {
-			const float *q = d->quads + 9 * (size_t)(g - ns);
-			for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, q + 3 * r, 12);
-			o[3] = PRIM_TAG_QUAD;
-			mat[j] = d->quad_mat[g - ns];
-		} else {
-			const float *t = d->triangles + 9 * (size_t)(g - ns - nq);
-			for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, t + 3 * r, 12);
-			o[3] = PRIM_TAG_TRI;
-			mat[j] = d->triangle_mat[g - ns - nq];
-			if (!tri_uv.empty()) std::memcpy(&tri_uv[6 * (size_t)j], d->triangle_uv + 6 * (size_t)(g - ns - nq), 24);
+	parallel_ranges((size_t)n, [&](size_t j0, size_t j1) {
+		for (size_t j = j0; j < j1; ++j) {
+			const int32_t g = bvh.order[j];
+			float *o = &prims[12 * j];
+			gid[j] = g;
+			if (g < ns) {
+				std::memcpy(o, d->spheres + 4 * (size_t)g, 16);
+				mat[j] = d->sphere_mat[g];
+			} else if (g < ns + nq) {
+				const float *q = d->quads + 9 * (size_t)(g - ns);
+				for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, q + 3 * r, 12);
+				o[3] = PRIM_TAG_QUAD;
+				mat[j] = d->quad_mat[g - ns];
+			} else {
+				const float *t = d->triangles + 9 * (size_t)(g - ns - nq);
+				for (int r = 0; r < 3; ++r) std::memcpy(o + 4 * r, t + 3 * r, 12);
+				o[3] = PRIM_TAG_TRI;
+				mat[j] = d->triangle_mat[g - ns - nq];
+				if (!tri_uv.empty()) std::memcpy(&tri_uv[6 * j], d->triangle_uv + 6 * (size_t)(g - ns - nq), 24);
+			}
 		}
-	}
+	});
 
 	// the 4-wide tree: measured faster for the 2M-triangle mesh (trees deep in HBM: half the dependent
 	// node fetches), slower for sphere fields of up to 152k spheres and for trees held in shared memory
