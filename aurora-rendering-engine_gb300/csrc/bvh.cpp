@@ -26,6 +26,12 @@ struct TmpNode {
 	int32_t depth = 0;
 };
 
+// a range's box and its centroids' box; known once the parent's binning has them
+struct Bounds {
+	double lo[3], hi[3], clo[3], chi[3];
+	bool known = false;
+};
+
 constexpr int NBINS = 16;
 constexpr int32_t SEQUENTIAL_BUILD_MAX = 1 << 15;  // primitives below which one thread builds the tree
 
@@ -147,9 +153,13 @@ struct Builder {
 			}
 	}
 
-	// returns the split position (index in [first, first+count)) or -1 for a leaf
+	// returns the split position (index in [first, first+count)) or -1 for a
+	// leaf; kid[0], kid[1] get the two sides' bounds when the binned split
+	// is taken (unions of the bins': min and max are exact, so they equal
+	// a pass over the sides' primitives)
 	int32_t split(int32_t first, int32_t count, int depth, const double lo[3], const double hi[3],
-		const double clo[3], const double chi[3]) {
+		const double clo[3], const double chi[3], Bounds kid[2]) {
+		kid[0].known = kid[1].known = false;
 		if (count <= 1) return -1;
 		int axis = 0;
 		for (int k = 1; k < 3; ++k)
@@ -168,66 +178,95 @@ struct Builder {
 		if (!(ext > 0)) return count <= leaf_size ? -1 : median();
 		// binned SAH along the widest centroid axis
 		struct Bin {
-			double lo[3], hi[3];
+			double lo[3], hi[3], clo[3], chi[3];
 			int32_t n;
-		} bins[NBINS];
-		for (auto &b : bins) {
-			for (int k = 0; k < 3; ++k) b.lo[k] = std::numeric_limits<double>::infinity(), b.hi[k] = -b.lo[k];
-			b.n = 0;
-		}
+		};
+		// the bins in use (bit b of `used`), each set by its first primitive:
+		// min and max of one value are the value, and empty bins change no
+		// union, so only used bins are visited
+		struct BinSet {
+			Bin bin[NBINS];
+			uint32_t used = 0;
+			void add(int b, const double *lo, const double *hi, const double *cc) {
+				Bin &x = bin[b];
+				if (!(used >> b & 1u)) {
+					used |= 1u << b;
+					for (int k = 0; k < 3; ++k) x.lo[k] = lo[k], x.hi[k] = hi[k], x.clo[k] = x.chi[k] = cc[k];
+					x.n = 1;
+					return;
+				}
+				for (int k = 0; k < 3; ++k) {
+					x.lo[k] = std::min(x.lo[k], lo[k]), x.hi[k] = std::max(x.hi[k], hi[k]);
+					x.clo[k] = std::min(x.clo[k], cc[k]), x.chi[k] = std::max(x.chi[k], cc[k]);
+				}
+				++x.n;
+			}
+			void merge(const BinSet &o) {
+				for (uint32_t m = o.used; m; m &= m - 1) {
+					const int b = __builtin_ctz(m);
+					const Bin &y = o.bin[b];
+					if (!(used >> b & 1u)) {
+						used |= 1u << b;
+						bin[b] = y;
+						continue;
+					}
+					Bin &x = bin[b];
+					for (int k = 0; k < 3; ++k) {
+						x.lo[k] = std::min(x.lo[k], y.lo[k]), x.hi[k] = std::max(x.hi[k], y.hi[k]);
+						x.clo[k] = std::min(x.clo[k], y.clo[k]), x.chi[k] = std::max(x.chi[k], y.chi[k]);
+					}
+					x.n += y.n;
+				}
+			}
+		};
 		double scale = NBINS / ext;
 		auto bin_of = [&](int32_t p) {
 			int b = (int)((cen[3 * p + axis] - clo[axis]) * scale);
 			return std::min(std::max(b, 0), NBINS - 1);
 		};
-		// chunk-local bins: on the stack for one chunk, on the heap for the few large ranges
-		std::array<Bin, NBINS> local_bins;
-		std::vector<std::array<Bin, NBINS>> heap_bins(count >= PAR_RANGE ? 32 : 0);
-		auto bins_of = [&](int c) -> std::array<Bin, NBINS> & { return heap_bins.empty() ? local_bins : heap_bins[c]; };
+		// one range: binned straight into `bins`; the few large ranges: chunk-local bins on the heap, merged
+		BinSet bins;
+		std::vector<BinSet> heap_bins(count >= PAR_RANGE ? 32 : 0);
+		auto bins_of = [&](int c) -> BinSet & { return heap_bins.empty() ? bins : heap_bins[c]; };
 		const int nc = chunked(first, count, [&](int32_t b0, int32_t b1, int c) {
-			std::array<Bin, NBINS> &lb = bins_of(c);
-			for (auto &b : lb) {
-				for (int k = 0; k < 3; ++k) b.lo[k] = std::numeric_limits<double>::infinity(), b.hi[k] = -b.lo[k];
-				b.n = 0;
-			}
+			BinSet &lb = bins_of(c);
+			lb.used = 0;
 			for (int32_t i = b0; i < b1; ++i) {
-				Bin &b = lb[bin_of(idx[i])];
-				const PrimBox &pb = boxes[idx[i]];
-				for (int k = 0; k < 3; ++k) b.lo[k] = std::min(b.lo[k], pb.lo[k]), b.hi[k] = std::max(b.hi[k], pb.hi[k]);
-				++b.n;
+				const int32_t p = idx[i];
+				lb.add(bin_of(p), boxes[p].lo, boxes[p].hi, &cen[3 * (size_t)p]);
 			}
 		});
-		for (int c = 0; c < nc; ++c) {
-			const std::array<Bin, NBINS> &cb = bins_of(c);
-			for (int b = 0; b < NBINS; ++b) {
-				for (int k = 0; k < 3; ++k)
-					bins[b].lo[k] = std::min(bins[b].lo[k], cb[b].lo[k]), bins[b].hi[k] = std::max(bins[b].hi[k], cb[b].hi[k]);
-				bins[b].n += cb[b].n;
-			}
-		}
+		if (!heap_bins.empty())
+			for (int c = 0; c < nc; ++c) bins.merge(heap_bins[c]);
+		// SAH sweep over the used bins.  Candidate i splits between used bins
+		// occ[i - 1] and occ[i]; every split position in that gap gives the same
+		// two sides, and the first, occ[i - 1] + 1, is the one a sweep over all
+		// positions keeps (the first minimum wins).
+		int occ[NBINS], m = 0;
+		for (uint32_t u = bins.used; u; u &= u - 1) occ[m++] = __builtin_ctz(u);
 		double right_area[NBINS];
 		int32_t right_n[NBINS];
 		double rlo[3], rhi[3];
 		for (int k = 0; k < 3; ++k) rlo[k] = std::numeric_limits<double>::infinity(), rhi[k] = -rlo[k];
 		int32_t rn = 0;
-		for (int b = NBINS - 1; b > 0; --b) {
-			for (int k = 0; k < 3; ++k) rlo[k] = std::min(rlo[k], bins[b].lo[k]), rhi[k] = std::max(rhi[k], bins[b].hi[k]);
-			rn += bins[b].n;
-			right_area[b] = area(rlo, rhi);
-			right_n[b] = rn;
+		for (int i = m - 1; i > 0; --i) {
+			const Bin &x = bins.bin[occ[i]];
+			for (int k = 0; k < 3; ++k) rlo[k] = std::min(rlo[k], x.lo[k]), rhi[k] = std::max(rhi[k], x.hi[k]);
+			rn += x.n;
+			right_area[i] = area(rlo, rhi);
+			right_n[i] = rn;
 		}
 		double llo[3], lhi[3];
 		for (int k = 0; k < 3; ++k) llo[k] = std::numeric_limits<double>::infinity(), lhi[k] = -llo[k];
 		int32_t ln = 0;
 		double best = std::numeric_limits<double>::infinity();
 		int best_b = -1;
-		for (int b = 1; b < NBINS; ++b) {
-			for (int k = 0; k < 3; ++k)
-				llo[k] = std::min(llo[k], bins[b - 1].lo[k]), lhi[k] = std::max(lhi[k], bins[b - 1].hi[k]);
-			ln += bins[b - 1].n;
-			if (ln == 0 || right_n[b] == 0) continue;
-			double c = area(llo, lhi) * ln + right_area[b] * right_n[b];
-			if (c < best) best = c, best_b = b;
+		for (int i = 1; i < m; ++i) {
+			const Bin &x = bins.bin[occ[i - 1]];
+			for (int k = 0; k < 3; ++k) llo[k] = std::min(llo[k], x.lo[k]), lhi[k] = std::max(lhi[k], x.hi[k]);
+			ln += x.n;
+			double c = area(llo, lhi) * ln + right_area[i] * right_n[i];
+			if (c < best) best = c, best_b = occ[i - 1] + 1;
 		}
 		double parent = area(lo, hi);
 		double leaf_cost = (double)count;
@@ -243,6 +282,20 @@ struct Builder {
 			mid = (int32_t)(it - idx.begin());
 		}
 		if (mid == first || mid == first + count) return median();
+		for (int side = 0; side < 2; ++side) {
+			Bounds &w = kid[side];
+			for (int k = 0; k < 3; ++k)
+				w.lo[k] = w.clo[k] = std::numeric_limits<double>::infinity(), w.hi[k] = w.chi[k] = -w.lo[k];
+		}
+		for (int i = 0; i < m; ++i) {
+			const Bin &x = bins.bin[occ[i]];
+			Bounds &w = kid[occ[i] < best_b ? 0 : 1];
+			for (int k = 0; k < 3; ++k) {
+				w.lo[k] = std::min(w.lo[k], x.lo[k]), w.hi[k] = std::max(w.hi[k], x.hi[k]);
+				w.clo[k] = std::min(w.clo[k], x.clo[k]), w.chi[k] = std::max(w.chi[k], x.chi[k]);
+			}
+		}
+		kid[0].known = kid[1].known = true;
 		return mid;
 	}
 
@@ -256,10 +309,11 @@ struct Builder {
 		nodes.reserve(2 * (size_t)n);
 		struct Job {
 			int32_t node, first, count, depth;
+			Bounds bounds;  // of [first, first + count), when the parent's split knew them
 		};
 		if (n < SEQUENTIAL_BUILD_MAX) {
 			// small scenes: the whole tree on this thread (starting threads would cost more)
-			std::vector<Job> st{ { 0, 0, n, 0 } };
+			std::vector<Job> st{ { 0, 0, n, 0, {} } };
 			nodes.push_back(TmpNode{});
 			while (!st.empty()) {
 				Job j = st.back();
@@ -278,19 +332,20 @@ struct Builder {
 		static const int n_hw = (int)hw_threads();
 		const int32_t par_min = std::max<int32_t>(4096, n / (4 * n_hw));
 		std::vector<Job> deferred;
-		std::vector<Job> level{ { 0, 0, n, 0 } };
+		std::vector<Job> level{ { 0, 0, n, 0, {} } };
 		nodes.push_back(TmpNode{});
 		while (!level.empty()) {
 			std::vector<int32_t> mids(level.size());
+			std::vector<std::array<Bounds, 2>> kid_bounds(level.size());
 			auto split_job = [&](size_t k) {
 				const Job &j = level[k];
-				double lo[3], hi[3], clo[3], chi[3];
-				bounds(j.first, j.count, lo, hi, clo, chi);
+				Bounds bb = j.bounds;
+				if (!bb.known) bounds(j.first, j.count, bb.lo, bb.hi, bb.clo, bb.chi);
 				TmpNode &t = nodes[j.node];
-				std::memcpy(t.lo, lo, sizeof lo);
-				std::memcpy(t.hi, hi, sizeof hi);
+				std::memcpy(t.lo, bb.lo, sizeof bb.lo);
+				std::memcpy(t.hi, bb.hi, sizeof bb.hi);
 				t.depth = j.depth;
-				mids[k] = split(j.first, j.count, j.depth, lo, hi, clo, chi);
+				mids[k] = split(j.first, j.count, j.depth, bb.lo, bb.hi, bb.clo, bb.chi, kid_bounds[k].data());
 			};
 			if ((int)level.size() >= n_hw) {
 				std::atomic<size_t> next{ 0 };
@@ -321,8 +376,8 @@ struct Builder {
 				nodes.push_back(TmpNode{});
 				nodes[j.node].left = l;
 				nodes[j.node].right = l + 1;
-				const Job kids[2] = { { l, j.first, mid - j.first, j.depth + 1 },
-					{ l + 1, mid, j.first + j.count - mid, j.depth + 1 } };
+				const Job kids[2] = { { l, j.first, mid - j.first, j.depth + 1, kid_bounds[k][0] },
+					{ l + 1, mid, j.first + j.count - mid, j.depth + 1, kid_bounds[k][1] } };
 				for (const Job &c : kids) {
 					if (c.count < par_min && c.count > leaf_size)
 						deferred.push_back(c);
@@ -341,8 +396,9 @@ struct Builder {
 			for (size_t k; (k = next_job.fetch_add(1)) < deferred.size();) {
 				std::vector<TmpNode> &ln = local[k];
 				std::vector<Job> st;
+				ln.reserve(2 * (size_t)deferred[k].count);  // a binary tree over count primitives, leaves of one or more
 				ln.push_back(TmpNode{});
-				st.push_back({ 0, deferred[k].first, deferred[k].count, deferred[k].depth });
+				st.push_back({ 0, deferred[k].first, deferred[k].count, deferred[k].depth, deferred[k].bounds });
 				while (!st.empty()) {
 					Job j = st.back();
 					st.pop_back();
@@ -384,14 +440,15 @@ struct Builder {
 	// one step of the build: bounds and split of job j's range into node j.node of `ns`
 	template <class JobT>
 	void expand(const JobT &j, std::vector<TmpNode> &ns, std::vector<JobT> &stack, int &depth_max) {
-		double lo[3], hi[3], clo[3], chi[3];
-		bounds(j.first, j.count, lo, hi, clo, chi);
+		Bounds bb = j.bounds;
+		if (!bb.known) bounds(j.first, j.count, bb.lo, bb.hi, bb.clo, bb.chi);
 		TmpNode &t = ns[j.node];
-		std::memcpy(t.lo, lo, sizeof lo);
-		std::memcpy(t.hi, hi, sizeof hi);
+		std::memcpy(t.lo, bb.lo, sizeof bb.lo);
+		std::memcpy(t.hi, bb.hi, sizeof bb.hi);
 		t.depth = j.depth;
 		depth_max = std::max(depth_max, j.depth);
-		int32_t mid = split(j.first, j.count, j.depth, lo, hi, clo, chi);
+		Bounds kid[2];
+		int32_t mid = split(j.first, j.count, j.depth, bb.lo, bb.hi, bb.clo, bb.chi, kid);
 		if (mid < 0) {
 			ns[j.node].first = j.first;
 			ns[j.node].count = j.count;
@@ -402,8 +459,8 @@ struct Builder {
 		ns.push_back(TmpNode{});
 		ns[j.node].left = l;
 		ns[j.node].right = l + 1;
-		stack.push_back({ l + 1, mid, j.first + j.count - mid, j.depth + 1 });
-		stack.push_back({ l, j.first, mid - j.first, j.depth + 1 });
+		stack.push_back({ l + 1, mid, j.first + j.count - mid, j.depth + 1, kid[1] });
+		stack.push_back({ l, j.first, mid - j.first, j.depth + 1, kid[0] });
 	}
 };
 
