@@ -390,10 +390,16 @@ struct Builder {
 		if (deferred.empty()) return;
 		std::vector<std::vector<TmpNode>> local(deferred.size());
 		std::vector<int> local_depth(deferred.size(), 0);
+		// largest subtrees first, so no large one starts last (each writes only its own list)
+		std::vector<size_t> by_size(deferred.size());
+		std::iota(by_size.begin(), by_size.end(), (size_t)0);
+		std::stable_sort(by_size.begin(), by_size.end(),
+			[&](size_t x, size_t y) { return deferred[x].count > deferred[y].count; });
 		std::atomic<size_t> next_job{ 0 };
 		auto worker = [&]() {
 			inline_passes() = true;  // whole subtrees per thread
-			for (size_t k; (k = next_job.fetch_add(1)) < deferred.size();) {
+			for (size_t q; (q = next_job.fetch_add(1)) < deferred.size();) {
+				const size_t k = by_size[q];
 				std::vector<TmpNode> &ln = local[k];
 				std::vector<Job> st;
 				ln.reserve(2 * (size_t)deferred[k].count);  // a binary tree over count primitives, leaves of one or more
