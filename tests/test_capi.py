@@ -76,6 +76,22 @@ def test_descriptor_validation(lib, case):
     assert msg
 
 
+def test_first_bad_triangle_is_reported_in_large_scenes(lib):
+    """Above 2^16 triangles the checks run on several threads; the message
+    still names the lowest-numbered bad triangle, as a serial scan would."""
+    n = 100_000
+    base = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], np.float32)
+    tris = np.tile(base, (n, 1)) + np.repeat(np.arange(n, dtype=np.float32) * 0.01, 9).reshape(n, 9)
+    tris[99_999, 4] = np.nan                        # non-finite vertex
+    tris[90_000, 3:6] = tris[90_000, 0:3]           # zero edge vector
+    tris[41_000, 6:9] = 2 * tris[41_000, 3:6] - tris[41_000, 0:3]  # collinear edges
+    s = are.SceneArrays()
+    m = s.material(are.MAT_LAMBERTIAN, albedo=(0.5, 0.5, 0.5))
+    s.add_triangles(tris.reshape(-1), m)
+    st, msg = _create(lib, s)
+    assert st == 1 and "triangle 41000" in msg and "collinear" in msg, (st, msg)
+
+
 def test_scene_create_without_device_is_an_error(lib):
     if lib.are_device_count() > 0:
         pytest.skip("a device is present")
