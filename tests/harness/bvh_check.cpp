@@ -19,6 +19,19 @@
 using are_core::BvhResult;
 using are_core::PrimBox;
 
+// FNV-1a over the bytes of both trees and the leaf order: a fingerprint of the build's decisions
+static unsigned long long fingerprint(const BvhResult &a, const std::vector<float> &w) {
+	unsigned long long x = 1469598103934665603ull;
+	auto mix = [&](const void *p, size_t n) {
+		const unsigned char *c = (const unsigned char *)p;
+		for (size_t i = 0; i < n; ++i) x = (x ^ c[i]) * 1099511628211ull;
+	};
+	mix(a.nodes.data(), a.nodes.size() * sizeof(float));
+	mix(a.order.data(), a.order.size() * sizeof(int32_t));
+	mix(w.data(), w.size() * sizeof(float));
+	return x;
+}
+
 int main(int argc, char **argv) {
 	const int n = argc > 1 ? std::atoi(argv[1]) : 200000;
 	const int leaf = argc > 2 ? std::atoi(argv[2]) : 4;
@@ -64,7 +77,8 @@ int main(int argc, char **argv) {
 	const std::vector<float> w = are_core::collapse_bvh4(a, 256);
 	if (ii(0, 7) > 0) {  // the binary root is a leaf: no wide tree
 		if (!w.empty()) { std::puts("FAIL wide tree over a single leaf"); return 1; }
-		std::printf("OK nodes %d depth %d max_leaf %d wide 0\n", a.n_nodes, a.depth, a.max_leaf);
+		std::printf("OK nodes %d depth %d max_leaf %d wide 0 fingerprint %016llx\n", a.n_nodes, a.depth, a.max_leaf,
+			fingerprint(a, w));
 		return 0;
 	}
 	if (w.size() % 32 != 0 || w.empty()) { std::puts("FAIL wide size"); return 1; }
@@ -164,6 +178,7 @@ int main(int argc, char **argv) {
 		// the wide walk skips collapsed levels, so it may enter a leaf whose binary ancestor it did not test
 		if (!std::includes(got.begin(), got.end(), want.begin(), want.end())) { std::puts("FAIL wide walk misses a leaf"); return 1; }
 	}
-	std::printf("OK nodes %d depth %d max_leaf %d wide %d leaves %d\n", a.n_nodes, a.depth, a.max_leaf, nw, leaves4);
+	std::printf("OK nodes %d depth %d max_leaf %d wide %d leaves %d fingerprint %016llx\n", a.n_nodes, a.depth, a.max_leaf,
+		nw, leaves4, fingerprint(a, w));
 	return 0;
 }

@@ -24,7 +24,17 @@ def harness(tmp_path_factory):
     return out
 
 
-@pytest.mark.parametrize("n,leaf", [(1, 4), (37, 4), (5000, 2), (300000, 4), (300000, 8)])
+# Fingerprints (FNV-1a over the binary nodes, the leaf order and the 4-wide
+# nodes) of the trees the builder made for these inputs with its append,
+# layout, 4-wide collapse and node bounds done serially, one pass per node:
+# the threaded phases and the bounds taken from the parent's bins must
+# reproduce those trees byte for byte.
+SERIAL_BUILD = {(1, 4): "c4fc79dec9708146", (37, 4): "36a1e945e89f77a2", (5000, 2): "f4e986d8a3b5046d",
+                (300000, 4): "679c4fc7a64617ca", (300000, 8): "679c4fc7a64617ca"}
+
+
+@pytest.mark.parametrize("n,leaf", sorted(SERIAL_BUILD))
 def test_build_is_deterministic_and_well_formed(harness, n, leaf):
     r = subprocess.run([str(harness), str(n), str(leaf)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
+    assert r.stdout.split("fingerprint")[1].split()[0] == SERIAL_BUILD[(n, leaf)], r.stdout
