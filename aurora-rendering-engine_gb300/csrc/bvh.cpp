@@ -518,20 +518,25 @@ BvhResult build_bvh(const std::vector<PrimBox> &boxes, int leaf_size) {
 	}
 	// Depth-first, the queued subtrees are laid out one after another, last
 	// queued first, each over a contiguous run of slots as long as its node
-	// count less one; so each is laid out on its own, in parallel.  Children
-	// always follow their parent in the build's list, so one backward pass
-	// counts every subtree's nodes.
+	// count less one: one parallel pass counts each subtree's nodes, a second
+	// lays each out on its own.
 	std::vector<std::pair<int32_t, int32_t>> dfs;  // (subtree root, first slot of its descendants)
-	if (!work.empty()) {
-		std::vector<int32_t> sub(ntmp, 1);
-		for (size_t t = ntmp; t-- > 0;) {
-			const TmpNode &tn = b.nodes[t];
-			if (tn.left >= 0) sub[t] = 1 + sub[tn.left] + sub[tn.right];
+	for (auto it = work.rbegin(); it != work.rend(); ++it) dfs.push_back({ *it, 0 });
+	run_jobs(dfs.size(), nthreads, [&](size_t k) {
+		std::vector<int32_t> st{ dfs[k].first };
+		int32_t c = 0;
+		while (!st.empty()) {
+			const TmpNode &tn = b.nodes[st.back()];
+			st.pop_back();
+			++c;
+			if (tn.left >= 0) st.push_back(tn.left), st.push_back(tn.right);
 		}
-		for (; !work.empty(); work.pop_back()) {
-			dfs.push_back({ work.back(), next });
-			next += sub[work.back()] - 1;
-		}
+		dfs[k].second = c;
+	});
+	for (auto &d : dfs) {
+		const int32_t c = d.second;
+		d.second = next;
+		next += c - 1;
 	}
 	run_jobs(dfs.size(), nthreads, [&](size_t k) {
 		std::vector<int32_t> st{ dfs[k].first };
