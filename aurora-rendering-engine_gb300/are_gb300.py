@@ -30,6 +30,7 @@ MAP_SURFACE_UV, MAP_SPHERICAL = 0, 1
 BG_CONSTANT, BG_SKY_GRADIENT = 0, 1
 TRI_REFERENCE_MT, TRI_WATERTIGHT = 0, 1
 BVH_HOST_SAH, BVH_DEVICE = 0, 1
+ACCEL_AUTO, ACCEL_BVH = 0, 1
 EST_PATH, EST_LEGACY_RT, EST_GUIDED = 0, 1, 2
 FLAG_DEVICE_OUTPUT, FLAG_NO_JITTER, FLAG_CLAMP_OUTPUT, FLAG_LEGACY_MT19937 = 1, 2, 4, 8
 CONFIG_RANDOM_SPHERES, CONFIG_CORNELL, CONFIG_MESH, CONFIG_CORNELL_OCCLUDED, CONFIG_LEGACY_RT = 0, 1, 2, 4, 5
@@ -77,6 +78,7 @@ class SceneArrays:
     bvh_leaf_size: int = 0
     bvh_build: int = 0
     bvh_width: int = 0
+    accel: int = 0
 
     @property
     def n_prims(self) -> int:
@@ -140,7 +142,7 @@ class SceneDesc(C.Structure):
         ("n_texels", C.c_int64), ("texels", _f),
         ("background", C.c_int32), ("bg_a", C.c_float * 3), ("bg_b", C.c_float * 3),
         ("triangle_test", C.c_int32), ("bvh_leaf_size", C.c_int32), ("bvh_build", C.c_int32),
-        ("bvh_width", C.c_int32)]
+        ("bvh_width", C.c_int32), ("accel", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -257,6 +259,7 @@ def desc_struct(s: SceneArrays) -> tuple[SceneDesc, list]:
     d.bvh_leaf_size = int(s.bvh_leaf_size)
     d.bvh_build = int(s.bvh_build)
     d.bvh_width = int(s.bvh_width)
+    d.accel = int(s.accel)
     return d, keep
 
 
@@ -285,6 +288,7 @@ def arrays_from_desc(d: SceneDesc) -> SceneArrays:
     s.background, s.bg_a, s.bg_b = d.background, tuple(d.bg_a), tuple(d.bg_b)
     s.triangle_test, s.bvh_leaf_size, s.bvh_build = d.triangle_test, d.bvh_leaf_size, d.bvh_build
     s.bvh_width = d.bvh_width
+    s.accel = d.accel
     return s
 
 

@@ -386,7 +386,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_init");
 	}
-	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const bool linear = sc->linear;
 	const void *isect_fn = linear ? (const void *)k_intersect_select<true> : (const void *)k_intersect_select<false>;
 	const int g_int = grid_of(isect_fn, sc->n_sms);
 	const int g_sh = grid_of((const void *)k_shade_guided, sc->n_sms);

@@ -2,28 +2,31 @@
 // a fixed, statically sized device array instead of allocated memory.
 //
 // Who needs it: code that renders where it may not allocate device memory —
-// for example inside a CUDA stream capture the application is recording
-// (cudaMalloc/cudaFree would break or end that capture), or inside a plugin
-// host that hands a plugin a fixed device-memory budget and forbids it from
-// allocating on its own.  Such a caller creates the scene beforehand (scene
-// creation does allocate) and then renders with this entry point, which
-// calls no cudaMalloc, no cudaFree, no allocating library routine, and
-// creates no events, streams or graphs.
+// a plugin host that hands a plugin a fixed device-memory budget and forbids
+// it from allocating on its own, or an application that owns all device
+// memory through its own allocator and must not meet the device-wide
+// synchronisation of a cudaMalloc/cudaFree in the middle of a frame.  Such a
+// caller creates the scene beforehand (scene creation does allocate) and then
+// renders with this entry point, which calls no cudaMalloc, no cudaFree, no
+// allocating library routine, and creates no events, streams or graphs.  The
+// render runs on the scene's own stream and the call returns when it is done.
 //
-// The scratch — the path pool, its queues and accumulators, and one work
-// item per pixel — lives in g_noalloc_scratch below (ARE_NOALLOC_SCRATCH_BYTES).
-// Both schedules of are_render run here (params->schedule; the megakernel is
-// one launch of k_tail with at most ARE_NOALLOC_MAX_PATHS paths).
+// The scratch — the path pool, its queues and accumulators, and the work
+// items (pixel x chunk of samples) — lives in g_noalloc_scratch below
+// (ARE_NOALLOC_SCRATCH_BYTES).  Both schedules of are_render run here
+// (params->schedule; the megakernel is one launch of k_tail with at most
+// ARE_NOALLOC_MAX_PATHS paths).
 // The array belongs to the library's device module: every GPU that loads the
 // library holds it until the process exits.  Kernels receive its address; host
 // code never dereferences the symbol (on the host, the name is only a
 // stand-in for the device array), so the address is looked up once per device
 // with cudaGetSymbolAddress, with that device current, on the first call made
-// on that device.  That first call should therefore come before any stream
-// capture.  All calls share the one array and it keeps the last call's
-// contents; everything that must start at zero is cleared by each call, and
-// calls whose work overlaps on the GPU (two streams, two host threads) race on
-// it: serialise them.
+// on that device, and kept for the life of the process (a cudaDeviceReset of
+// that device invalidates it; calls after one are not supported).  That first
+// call should therefore come before any stream capture.  All calls share the
+// one array and it keeps the last call's contents; everything that must start
+// at zero is cleared by each call, and calls whose work overlaps on the GPU
+// (two streams, two host threads) race on it: serialise them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -93,6 +96,8 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	are_render_stats *stats) {
 	if (!sc || !cam || !prm || !rgb) return bad("null scene, camera, params or output");
 	const are_render_params &p = *prm;
+	if (!(p.flags & ARE_FLAG_DEVICE_OUTPUT))
+		return bad("are_render_noalloc writes device buffers only: set ARE_FLAG_DEVICE_OUTPUT and pass device pointers");
 	if (p.estimator != ARE_EST_PATH) return bad("are_render_noalloc renders the path estimator only");
 	if (p.width <= 0 || p.height <= 0 || p.spp <= 0 || p.max_depth <= 0 || p.max_depth > 255)
 		return bad("width, height, spp must be > 0 and max_depth in [1, 255]");
@@ -106,18 +111,23 @@ are_status render_noalloc(are_scene *sc, const are_camera *cam, const are_render
 	if (p.schedule < ARE_SCHEDULE_AUTO || p.schedule > ARE_SCHEDULE_MEGAKERNEL) return bad("unknown schedule");
 	if (cudaSetDevice(sc->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
-	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const bool linear = sc->linear;
 	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
 	unsigned char *base = nullptr;
 	if (are_status st = scratch_address(sc->device, &base)) return st;
 
-	// one work item per pixel: the slot that renders a pixel runs all its samples
+	// work items are (pixel, chunk of samples), as in are_render; the automatic chunk is the smallest
+	// whose items fit the array, so small images still spread over many paths
 	Wave W{};
 	W.npix = p.width * p.height;
 	W.spp = p.spp;
-	W.chunk = p.spp;
-	W.nchunk = 1;
-	W.n_items = W.npix;
+	const int64_t max_chunks = ARE_NOALLOC_MAX_PIXELS / W.npix;  // >= 1: the pixel count was checked above
+	W.chunk = p.chunk > 0 ? std::min(p.chunk, p.spp) : (int)((p.spp + max_chunks - 1) / max_chunks);
+	W.nchunk = (p.spp + W.chunk - 1) / W.chunk;
+	W.n_items = (int64_t)W.npix * W.nchunk;
+	if (W.n_items > ARE_NOALLOC_MAX_PIXELS)
+		return bad("chunk " + std::to_string(W.chunk) + " gives " + std::to_string(W.n_items) +
+			" work items; are_render_noalloc handles at most " + std::to_string(ARE_NOALLOC_MAX_PIXELS));
 	// megakernel: at most one path per resident thread of its persistent grid
 	int P = p.pool_size > 0 ? p.pool_size : mega ? std::min(ARE_NOALLOC_MAX_PATHS, g_tail * BLOCK) : ARE_NOALLOC_MAX_PATHS;
 	P = (int)std::min<int64_t>(P, W.n_items);

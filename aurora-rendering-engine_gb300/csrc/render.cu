@@ -434,7 +434,7 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	// measured on GB300, the megakernel is the faster schedule on every workload scene (the path
 	// state stays in registers; no queue records go through memory between bounces)
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
-	const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+	const bool linear = sc->linear;
 	const int g_int = intersect_grid(linear, sc->dev, sc->n_sms);
 	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
 	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
@@ -694,7 +694,7 @@ are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, i
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
 	if (!st) {
-		const bool linear = sc->dev.n_prims <= LINEAR_MAX;
+		const bool linear = sc->linear;
 		int grid = grid_for(linear ? (const void *)k_intersect_batch<true> : (const void *)k_intersect_batch<false>,
 			sc->n_sms);
 		grid = (int)std::min<int64_t>(grid, (n + BLOCK - 1) / BLOCK);

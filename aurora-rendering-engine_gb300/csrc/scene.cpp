@@ -187,6 +187,7 @@ are_status validate(const are_scene_desc *d) {
 	if (d->background != ARE_BG_CONSTANT && d->background != ARE_BG_SKY_GRADIENT) return invalid("unknown background");
 	if (d->bvh_build != ARE_BVH_HOST_SAH && d->bvh_build != ARE_BVH_DEVICE) return invalid("unknown bvh_build");
 	if (d->bvh_width != 0 && d->bvh_width != 2 && d->bvh_width != 4) return invalid("bvh_width must be 0, 2 or 4");
+	if (d->accel != ARE_ACCEL_AUTO && d->accel != ARE_ACCEL_BVH) return invalid("unknown accel");
 	if (d->bvh_width == 4 && d->bvh_build == ARE_BVH_DEVICE)
 		return invalid("bvh_width 4 needs the host build (the device build's tree is traversed two-wide)");
 	if (d->triangle_test != ARE_TRI_REFERENCE_MT && d->triangle_test != ARE_TRI_WATERTIGHT)
@@ -447,7 +448,8 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	const bool four = d->bvh_width == 4 || (d->bvh_width == 0 && n > WIDE_BVH_MIN_PRIMS);
 	if (n > LINEAR_MAX && four) wide = collapse_bvh4(bvh, SMEM_NODES4);
 	std::vector<float> leaves;
-	if (n > 0 && n <= LINEAR_MAX)
+	const bool linear = n <= LINEAR_MAX && d->accel != ARE_ACCEL_BVH;
+	if (n > 0 && linear)
 		for (int32_t i = 0; i < bvh.n_nodes; ++i) {
 			int32_t cnt;
 			std::memcpy(&cnt, &bvh.nodes[8 * (size_t)i + 7], 4);
@@ -455,6 +457,7 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 		}
 
 	are_scene *sc = new are_scene();
+	sc->linear = linear;
 	cudaGetDevice(&sc->device);
 	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
 	DevScene &S = sc->dev;

@@ -15,6 +15,7 @@ struct are_scene {
 	int device = 0;
 	int n_sms = 0;
 	int64_t n_prims = 0, n_nodes = 0;
+	bool linear = false;  // closest hits by the linear scan of staged primitives (else the BVH)
 	int32_t n_spheres = 0, n_quads = 0, n_triangles = 0;
 	int32_t max_leaf = 0, depth = 0;
 	float box_lo[3] = { 0, 0, 0 }, box_hi[3] = { 0, 0, 0 };  // bounds of all primitives

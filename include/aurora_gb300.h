@@ -118,7 +118,14 @@ typedef struct are_scene_desc {
 	int32_t bvh_build;          /* ARE_BVH_*: where the tree is built (same answers either way) */
 	int32_t bvh_width;          /* children per BVH node traversed: 0 = automatic (4 above 2^19 primitives,
 	                               else 2), 2, or 4 (host build only); same answers either way */
+	int32_t accel;              /* ARE_ACCEL_*: how closest hits are found (same answers either way) */
 } are_scene_desc;
+
+enum {
+	ARE_ACCEL_AUTO = 0,  /* scenes of at most 48 primitives: a warp-cooperative linear scan of the
+	                        primitives staged in shared memory; larger scenes: the BVH */
+	ARE_ACCEL_BVH = 1    /* always traverse the BVH, whatever the scene's size */
+};
 
 enum {
 	ARE_BVH_HOST_SAH = 0,  /* binned SAH on the host (best trees; seconds for millions of primitives) */
@@ -241,29 +248,36 @@ ARE_API are_status are_intersect(are_scene *scene, const float *rays, int64_t n,
 /* ---- rendering without allocating -------------------------------------- */
 
 /* No counterpart in the reference: an extra entry point for callers that may
- * not allocate device memory while they render — for example code recording
- * its own CUDA stream capture, where cudaMalloc/cudaFree would break the
- * capture, or a plugin host that gives a plugin a fixed device-memory budget
- * and forbids allocations of its own.  Such a caller creates the scene first
+ * not allocate device memory while they render — for example a plugin host
+ * that hands each plugin a fixed device-memory budget and forbids allocations
+ * of its own, or an application whose memory is owned by its own allocator and
+ * that must not see the device-wide synchronisation a cudaMalloc/cudaFree can
+ * cause in the middle of a frame.  Such a caller creates the scene first
  * (are_scene_create allocates) and then calls are_render_noalloc, which
- * renders the path estimator (ARE_EST_PATH, either schedule) like are_render but calls no
- * cudaMalloc, cudaFree or other allocating routine and creates no streams,
- * events or graphs.
+ * renders the path estimator (ARE_EST_PATH, either schedule) like are_render
+ * but calls no cudaMalloc, cudaFree or other allocating routine and creates
+ * no streams, events or graphs.  The render runs on the scene's own stream and
+ * the call returns when it is done.
  *
- * Its scratch — at most ARE_NOALLOC_MAX_PATHS paths in flight and one work
- * item per pixel for at most ARE_NOALLOC_MAX_PIXELS pixels — is one static
- * device array of ARE_NOALLOC_SCRATCH_BYTES in the library, which every GPU
- * that loads the library holds until the process exits.  Larger images are
- * rejected with ARE_ERR_INVALID_ARGUMENT.
+ * Its scratch — at most ARE_NOALLOC_MAX_PATHS paths in flight and at most
+ * ARE_NOALLOC_MAX_PIXELS work items (a work item is one pixel's chunk of
+ * samples) — is one static device array of ARE_NOALLOC_SCRATCH_BYTES in the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Larger images, or a params->chunk that gives more work items, are
+ * rejected with ARE_ERR_INVALID_ARGUMENT.  params->chunk = 0 picks the
+ * smallest chunk whose work items fit; the result equals are_render's with
+ * the same chunk.
  *
  * rgb_out (required) and var_out (optional) are DEVICE pointers of
- * width*height*3 floats.  The result equals are_render's with chunk = spp.
- * The first call on a device looks up the array's device address (with that
- * device current); make that first call before any stream capture.  All calls
- * share the array and it keeps the last call's contents (each call clears what
- * must start at zero); calls that overlap on the GPU race on it, so serialise
- * them.  Statistics report counts; device_ms and kernel_ms stay 0 because no
- * events are created. */
+ * width*height*3 floats, and params->flags must include
+ * ARE_FLAG_DEVICE_OUTPUT (host pointers are rejected).  The first call on a
+ * device looks up the array's device address (with that device current) and
+ * keeps it for the life of the process; make that first call before any stream
+ * capture, and do not call this entry point after a cudaDeviceReset of that
+ * device.  All calls share the array and it keeps the last call's contents
+ * (each call clears what must start at zero); calls that overlap on the GPU
+ * race on it, so serialise them.  Statistics report counts; device_ms and
+ * kernel_ms stay 0 because no events are created. */
 #define ARE_NOALLOC_MAX_PATHS 65536
 #define ARE_NOALLOC_MAX_PIXELS 524288
 #define ARE_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)

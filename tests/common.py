@@ -56,3 +56,29 @@ def random_rays(n: int, seed: int, lo=-1.2, hi=1.2, t_min=REF_T_MIN, t_max=REF_T
 
 def hit_ids(h: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(h[:, 1]).view(np.int32)
+
+
+def sigma_test(m1, v1, m2, v2):
+    """Fraction of pixel channels whose means differ by more than 3 standard
+    errors of their difference; channels with zero variance on both sides must
+    match to 1e-5 relative.  Returns (fraction, zero-variance mismatches)."""
+    sd = np.sqrt(v1 + v2)
+    z = np.abs(m1 - m2)
+    flat = sd == 0
+    bad_flat = flat & (z > 1e-5 * np.maximum(1.0, np.abs(m1)))
+    out = ~flat & (z > 3 * sd)
+    return (out.sum() + bad_flat.sum()) / m1.size, bad_flat.sum()
+
+
+def binomial_bound(n, p=0.0027, k=5.0):
+    """Upper bound on the failure fraction of n independent 3-sigma tests
+    (expected 0.27 % under the null), k binomial standard deviations above."""
+    return p + k * np.sqrt(p * (1 - p) / n)
+
+
+def same_seed_agreement(m_gpu, m_cpu, rel=1e-4):
+    """Fractions of pixel channels that are bit-identical and that agree to
+    `rel` relative (floor 1e-3 absolute scale) between two same-seed renders."""
+    same = (m_gpu.view(np.uint32) == m_cpu.view(np.uint32)).mean()
+    close = (np.abs(m_gpu - m_cpu) <= rel * np.maximum(1e-3, np.abs(m_cpu))).mean()
+    return float(same), float(close)

@@ -40,7 +40,7 @@ def _create(lib, s):
 
 @pytest.mark.parametrize("case", ["null_tri_material", "zero_edge", "collinear", "bad_sphere", "bad_texture",
                                   "bad_image", "bad_mat_type", "degenerate_quad", "bad_bvh_width",
-                                  "wide_device_build", "bad_filter"])
+                                  "wide_device_build", "bad_filter", "bad_accel"])
 def test_descriptor_validation(lib, case):
     """Mirrors are::Triangle's constructor checks (src/object/triangle.cpp:9-46)
     and are::Texture's size check (src/texture.cpp:52-55); validation runs
@@ -67,6 +67,8 @@ def test_descriptor_validation(lib, case):
         s.bvh_width = 3
     elif case == "wide_device_build":  # the device build's tree is traversed two-wide only
         s.bvh_width, s.bvh_build = 4, are.BVH_DEVICE
+    elif case == "bad_accel":
+        s.accel = 5
     elif case == "bad_filter":
         s.texels = np.ones((4, 3), np.float32)
         t = s.texture(are.TEX_IMAGE, width=2, height=2, texel_offset=0)
