@@ -199,12 +199,13 @@ class TonemapParams(C.Structure):
 
 class GuideParams(C.Structure):
     _fields_ = [("mix", C.c_float), ("guide_depth", C.c_int32), ("train", C.c_int32), ("batch", C.c_int32),
-                ("lr", C.c_float), ("weight_clip", C.c_float), ("reserved_", C.c_int32 * 2)]
+                ("lr", C.c_float), ("weight_clip", C.c_float), ("cache_res", C.c_int32), ("reserved_", C.c_int32)]
 
     @staticmethod
-    def make(mix=0.5, guide_depth=2, train=1, batch=1 << 18, lr=1e-2, weight_clip=100.0) -> "GuideParams":
+    def make(mix=0.5, guide_depth=2, train=1, batch=1 << 18, lr=1e-2, weight_clip=100.0, cache_res=0) -> "GuideParams":
         g = GuideParams()
         g.mix, g.guide_depth, g.train, g.batch, g.lr, g.weight_clip = mix, guide_depth, train, batch, lr, weight_clip
+        g.cache_res = cache_res
         return g
 
 
@@ -357,6 +358,7 @@ def load(path: str | os.PathLike | None = None):
     L.are_guide_mixture.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.are_guide_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_void_p]
     L.are_guide_train.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.POINTER(C.c_float)]
+    L.are_guide_set_wait_limit.argtypes = [C.c_void_p, C.c_int32]
     for name in exported_symbols():
         fn = getattr(L, name)
         if fn.restype is C.c_int:  # are_status returns
@@ -537,6 +539,10 @@ class Guide:
         out = np.zeros(4096, np.float32)
         n = self.lib.are_guide_loss_history(self.h, out.ctypes.data, len(out))
         return list(out[:n])
+
+    def set_wait_limit(self, polls: int) -> None:
+        """are_guide_set_wait_limit: polls for the first tensor-core wait of each warpgroup (-1 = default)."""
+        check(self.lib.are_guide_set_wait_limit(self.h, int(polls)))
 
     def train(self, samples: np.ndarray, lr: float = 1e-2) -> float:
         samples = np.ascontiguousarray(samples, np.float32).reshape(-1, 13)

@@ -237,7 +237,10 @@ are_status render_batch(are_scene *const *scenes, const are_camera *cams, const 
 
 	cudaStream_t s = scenes[0]->stream;
 	cudaGetLastError();
-	st = cuda_status(cudaMemcpyAsync(d_table, table.data(), sizeof(BatchScene) * n, cudaMemcpyHostToDevice, s), "table");
+	// every scene's upload (asynchronous, on its own stream) has landed before the launch reads it
+	for (int i = 1; i < n && !st; ++i)
+		if (scenes[i]->stream != s) st = cuda_status(cudaStreamSynchronize(scenes[i]->stream), "scene upload");
+	if (!st) st = cuda_status(cudaMemcpyAsync(d_table, table.data(), sizeof(BatchScene) * n, cudaMemcpyHostToDevice, s), "table");
 	if (!st) st = cuda_status(cudaStreamSynchronize(s), "table");
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;

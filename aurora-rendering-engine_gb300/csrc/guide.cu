@@ -230,9 +230,11 @@ __device__ __forceinline__ void tc_mmas(uint32_t d_tmem, uint32_t a_addr, uint32
 			(accumulate || s > 0) ? 1u : 0u);
 }
 
+// first_limit: polls allowed for each warpgroup's first MMA wait (the others get TC_POLL_LIMIT); a
+// caller that wants to see the give-up path taken sets it to 0
 __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__restrict__ tc_img,
 	const float *__restrict__ feat, int n, const unsigned *__restrict__ n_dev, float *__restrict__ out,
-	unsigned *__restrict__ err, int mixture_out) {
+	unsigned *__restrict__ err, int mixture_out, uint32_t first_limit) {
 	extern __shared__ __align__(16) unsigned char smem[];
 	uint64_t *bar = reinterpret_cast<uint64_t *>(smem + TC_OFF_BAR);  // [0] weights, [1 + wg] MMAs of warpgroup wg
 	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1 + TC_WG);
@@ -295,11 +297,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_infer(const __half *__r
 	};
 	// one thread polls the mbarrier; the others sleep in the named barrier
 	// instead of spending issue slots the other warpgroups could use
+	uint32_t limit = min(first_limit, TC_POLL_LIMIT);
 	auto wait_mma = [&]() {
 		if (lt == 0) {
-			if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+			if (!mbar_wait(mbar, phase, limit)) fail[wg] = 1;
 			tc_fence_before();
 		}
+		limit = TC_POLL_LIMIT;
 		phase ^= 1u;
 		named_bar(bar_id, 128);
 		tc_fence_after();
@@ -794,7 +798,7 @@ are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_
 	const int tiles = (n + 127) / 128;
 	const int grid = std::max(1, std::min(n_sms, (tiles + TC_WG - 1) / TC_WG));
 	k_guide_infer<<<grid, TC_THREADS, guide_infer_smem(), s>>>(tc_img, d_feat, n, n_dev, d_out, d_err ? d_err : err_word,
-		mixture_out ? 1 : 0);
+		mixture_out ? 1 : 0, first_wait_limit);
 	return cuda_status(cudaGetLastError(), "k_guide_infer");
 }
 
@@ -1026,6 +1030,15 @@ ARE_API int32_t are_guide_loss_history(are_guide *gh, float *out, int32_t max) {
 	int32_t n = (int32_t)std::min<size_t>((size_t)max, g->loss_log.size());
 	std::memcpy(out, g->loss_log.data() + (g->loss_log.size() - n), n * sizeof(float));
 	return n;
+}
+
+ARE_API are_status are_guide_set_wait_limit(are_guide *gh, int32_t polls) {
+	return guard([&] {
+		GuideNet *g = reinterpret_cast<GuideNet *>(gh);
+		if (!g) return are_core::bad("null guide");
+		g->first_wait_limit = polls < 0 ? 0xffffffffu : (uint32_t)polls;
+		return ARE_OK;
+	});
 }
 
 ARE_API are_status are_guide_train(are_guide *gh, const float *samples, int64_t n, float lr, float *loss) {

@@ -39,6 +39,7 @@ struct GuideNet {
 	int64_t steps = 0;
 	float loss_scale = 8.0f;     // gradients are carried in FP16 times this factor
 	float weight_clip = 1e30f;   // cap on a sample's normalised weight
+	uint32_t first_wait_limit = 0xffffffffu;  // polls of each warpgroup's first MMA wait in inference (capped)
 	std::vector<float> loss_log; // losses of Adam steps taken inside renders
 
 	~GuideNet();
@@ -60,6 +61,9 @@ size_t guide_infer_smem();
 size_t guide_train_smem();
 
 are_status render_guided(struct ::are_scene *sc, GuideNet *net, const are_camera *cam, const are_render_params *prm,
+	const are_guide_params *gp, float *rgb, float *var, are_render_stats *stats);
+// the megakernel schedule of render_guided (guided_mega.cu), parameters validated by render_guided
+are_status render_guided_mega(struct ::are_scene *sc, GuideNet *net, const are_camera *cam, const are_render_params &p,
 	const are_guide_params *gp, float *rgb, float *var, are_render_stats *stats);
 
 }  // namespace are_core

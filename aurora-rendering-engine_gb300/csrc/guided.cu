@@ -297,7 +297,11 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	if (gp->train && (gp->batch < 256 || gp->batch > (1 << 20) || !(gp->lr > 0.f))) return bad("bad training batch or lr");
 	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");
 	if (net->device != sc->device) return bad("guide and scene live on different devices");
+	if (!(p.t_min >= 0.0f) || !std::isfinite(p.t_min)) return bad("t_min must be finite and >= 0");
+	if (p.schedule < ARE_SCHEDULE_AUTO || p.schedule > ARE_SCHEDULE_MEGAKERNEL) return bad("unknown schedule");
+	if (gp->cache_res < 0 || gp->cache_res > 128) return bad("cache_res must be in [0, 128]");
 	cudaSetDevice(sc->device);
+	if (p.schedule != ARE_SCHEDULE_WAVEFRONT) return render_guided_mega(sc, net, cam, p, gp, rgb, var, stats);
 
 	Wave W{};
 	W.npix = p.width * p.height;

@@ -542,10 +542,14 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	const unsigned tail_max = (unsigned)std::max<int64_t>(8192, P / 4);
 	const DevScene S = sc->dev;
 
-	unsigned init[8] = { (unsigned)std::min<int64_t>(P, W.n_items), 0u, 0u, (unsigned)std::min<int64_t>(P, W.n_items),
-		0u, 0u, 0u, 0u };
+	// the initial counters go up from the scene's pinned block (an asynchronous copy; the host does not
+	// touch words 0..7 again before the stream's next synchronisation)
+	unsigned *init = sc->host_counters;
+	for (int k = 0; k < 8; ++k) init[k] = 0u;
+	init[0] = init[3] = (unsigned)std::min<int64_t>(P, W.n_items);
 	cudaEventRecord(ev0, s);
-	st = cuda_status(cudaMemcpyAsync(W.cnt, init, sizeof init, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(counters)");
+	st = cuda_status(cudaMemcpyAsync(W.cnt, init, 8 * sizeof(unsigned), cudaMemcpyHostToDevice, s),
+		"cudaMemcpyAsync(counters)");
 	if (!st) st = cuda_status(cudaMemsetAsync(W.stat, 0, 8 * sizeof(unsigned long long), s), "cudaMemsetAsync(stats)");
 	if (!st) {
 		k_init<<<grid_for((const void *)k_init, sc->n_sms), BLOCK, 0, s>>>(W, (int)init[0]);
@@ -559,9 +563,8 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 		cudaEventRecord(kev[1], s);
 		++launches[ARE_KERNEL_OTHER];
 		st = cuda_status(cudaGetLastError(), "k_tail launch");
-		if (!st) st = cuda_status(cudaStreamSynchronize(s), "render");
-		float ms = 0.f;
-		if (!st && cudaEventElapsedTime(&ms, kev[0], kev[1]) == cudaSuccess) kms[ARE_KERNEL_OTHER] += ms;
+		// no synchronisation here: the resolve and the read-back follow in stream order, and the
+		// launch's time is read from its events after the render's one synchronisation
 	}
 	// capture GRAPH_ITERS iterations, each bracketed by timing events
 	if (!st && !mega) st = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -639,13 +642,24 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	unsigned long long hstat[3] = { 0, 0, 0 };
 	unsigned herr = 0;
 	if (!st) {
-		cudaMemcpyAsync(hstat, W.stat, sizeof hstat, cudaMemcpyDeviceToHost, s);
-		cudaMemcpyAsync(&herr, W.cnt + 4, sizeof herr, cudaMemcpyDeviceToHost, s);
+		// statistics and the error word come back through the pinned block (words 16..23 and 24)
+		unsigned long long *pstat = (unsigned long long *)(sc->host_counters + 16);
+		cudaMemcpyAsync(pstat, W.stat, sizeof hstat, cudaMemcpyDeviceToHost, s);
+		cudaMemcpyAsync(sc->host_counters + 24, W.cnt + 4, sizeof herr, cudaMemcpyDeviceToHost, s);
 		if (!dev_out) {
 			cudaMemcpyAsync(rgb, d_rgb, 3 * sizeof(float) * W.npix, cudaMemcpyDeviceToHost, s);
 			if (var) cudaMemcpyAsync(var, d_var, 3 * sizeof(float) * W.npix, cudaMemcpyDeviceToHost, s);
 		}
 		st = cuda_status(cudaStreamSynchronize(s), "render");
+		if (!st) {
+			for (int k = 0; k < 3; ++k) hstat[k] = pstat[k];
+			herr = sc->host_counters[24];
+		}
+	}
+	if (st) cudaStreamSynchronize(s);  // nothing of this render (the counter upload) is left in flight
+	if (mega && !st) {
+		float ms = 0.f;
+		if (cudaEventElapsedTime(&ms, kev[0], kev[1]) == cudaSuccess) kms[ARE_KERNEL_OTHER] += ms;
 	}
 	float total_ms = 0.f;
 	cudaEventElapsedTime(&total_ms, ev0, ev1);

@@ -41,13 +41,60 @@ bool g_pool_failed[256];
 std::mutex g_pinned_mu;
 std::vector<unsigned *> g_pinned_free;
 
-// small scenes are uploaded through one pinned staging buffer: one copy instead of one per array
+// small scenes are uploaded through one pinned staging buffer: one copy instead of one per array.  The
+// copy is not waited for: g_stage_done marks it, and the next scene waits for that event before it
+// overwrites the buffer, so a create-render-destroy frame synchronises once, in the render.
 constexpr size_t STAGE_BYTES = 8u << 20;
 std::mutex g_stage_mu;
 unsigned char *g_stage = nullptr;
+cudaEvent_t g_stage_done = nullptr;
 bool g_stage_failed = false;
 
+// Streams and timing events of destroyed scenes, per device, idle and ready for the next scene: a
+// caller that creates and destroys a scene every frame does not create a stream and events each time.
+struct SceneRuntime {
+	cudaStream_t stream;
+	std::vector<cudaEvent_t> events;
+};
+constexpr size_t RUNTIME_CACHE = 32;
+std::mutex g_runtime_mu;
+std::vector<SceneRuntime> g_runtime_free[256];
+
 }  // namespace
+
+// a stream (and the timing events that came with it) for a new scene on the current device
+static are_status acquire_runtime(are_scene *sc) {
+	if (sc->device >= 0 && sc->device < 256) {
+		std::lock_guard<std::mutex> lk(g_runtime_mu);
+		std::vector<SceneRuntime> &f = g_runtime_free[sc->device];
+		if (!f.empty()) {
+			sc->stream = f.back().stream;
+			sc->render_events = std::move(f.back().events);
+			f.pop_back();
+			return ARE_OK;
+		}
+	}
+	return cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+}
+
+// the idle stream and events of a scene being destroyed: kept for the next scene, or released
+static void release_runtime(are_scene *sc) {
+	if (!sc->stream) return;
+	if (sc->device >= 0 && sc->device < 256) {
+		std::lock_guard<std::mutex> lk(g_runtime_mu);
+		std::vector<SceneRuntime> &f = g_runtime_free[sc->device];
+		if (f.size() < RUNTIME_CACHE) {
+			f.push_back(SceneRuntime{ sc->stream, std::move(sc->render_events) });
+			sc->stream = nullptr;
+			sc->render_events.clear();
+			return;
+		}
+	}
+	for (cudaEvent_t e : sc->render_events) cudaEventDestroy(e);
+	sc->render_events.clear();
+	cudaStreamDestroy(sc->stream);
+	sc->stream = nullptr;
+}
 
 // Falls back to cudaMalloc (recorded in sc->allocations) if the device has no
 // pool support.
@@ -314,7 +361,7 @@ are_status scene_create_device(const are_scene_desc *d, are_scene **out) {
 	are_scene *sc = new are_scene();
 	cudaGetDevice(&sc->device);
 	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
-	are_status st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	are_status st = acquire_runtime(sc);
 	void *tmp = nullptr;
 	const size_t rec_b = ((48 * (size_t)n + 255) & ~(size_t)255), mat_b = ((4 * (size_t)n + 255) & ~(size_t)255);
 	if (!st) st = cuda_status(cudaMalloc(&tmp, rec_b + mat_b + 24 * uv.size() / 6), "cudaMalloc(scene upload)");
@@ -461,7 +508,7 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	cudaGetDevice(&sc->device);
 	cudaDeviceGetAttribute(&sc->n_sms, cudaDevAttrMultiProcessorCount, sc->device);
 	DevScene &S = sc->dev;
-	are_status st = cuda_status(cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+	are_status st = acquire_runtime(sc);
 	if (!st && !(sc->host_counters = pinned_block_acquire())) {
 		set_error("pinned host memory for the render counters");
 		st = ARE_ERR_OUT_OF_MEMORY;
@@ -490,16 +537,22 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	bool staged = false;
 	if (!st && total <= STAGE_BYTES) {
 		std::lock_guard<std::mutex> lk(g_stage_mu);
-		if (!g_stage && !g_stage_failed && cudaMallocHost((void **)&g_stage, STAGE_BYTES) != cudaSuccess) {
-			cudaGetLastError();
-			g_stage = nullptr;
-			g_stage_failed = true;
+		if (!g_stage && !g_stage_failed) {
+			if (cudaMallocHost((void **)&g_stage, STAGE_BYTES) != cudaSuccess ||
+				cudaEventCreateWithFlags(&g_stage_done, cudaEventDisableTiming) != cudaSuccess) {
+				cudaGetLastError();
+				if (g_stage) cudaFreeHost(g_stage);
+				g_stage = nullptr;
+				g_stage_failed = true;
+			}
 		}
 		if (g_stage) {
+			// the previous scene's copy out of the buffer must have finished
+			st = cuda_status(cudaEventSynchronize(g_stage_done), "scene upload");
 			for (const Part &q : parts)
-				if (q.bytes) std::memcpy(g_stage + q.off, q.src, q.bytes);
-			st = cuda_status(cudaMemcpyAsync(block, g_stage, total, cudaMemcpyHostToDevice, sc->stream), "scene upload");
-			if (!st) st = cuda_status(cudaStreamSynchronize(sc->stream), "scene upload");  // the buffer is reused
+				if (!st && q.bytes) std::memcpy(g_stage + q.off, q.src, q.bytes);
+			if (!st) st = cuda_status(cudaMemcpyAsync(block, g_stage, total, cudaMemcpyHostToDevice, sc->stream), "scene upload");
+			if (!st) st = cuda_status(cudaEventRecord(g_stage_done, sc->stream), "scene upload");
 			staged = true;
 		}
 	}
@@ -555,10 +608,11 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 are_scene::~are_scene() {
 	if (stream) cudaStreamSynchronize(stream);
 	if (render_exec) cudaGraphExecDestroy(render_exec);
-	for (cudaEvent_t e : render_events) cudaEventDestroy(e);
 	for (void *p : allocations) cudaFree(p);
 	// pool blocks (the scene arrays, the render workspace) go back to the pool in stream order
 	for (void *p : pool_allocations) cudaFreeAsync(p, stream);
+	// the host counters are read only after a synchronisation, and nothing of this scene is left in
+	// flight that writes them
 	are_core::pinned_block_release(host_counters);
-	if (stream) cudaStreamDestroy(stream);
+	are_core::release_runtime(this);
 }

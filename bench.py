@@ -528,13 +528,26 @@ def run_legacy(args, rank, world) -> None:
     sc.close()
 
 
+def workload_config(workload: str, par: dict, primitives: int, accel: str, bvh_build: str, world: int) -> dict:
+    """The `config` object of a render workload's line: the same keys and
+    values on the GPU arm and the reference arm."""
+    return {"workload": workload, "width": par["width"], "height": par["height"], "spp": par["spp"],
+            "max_depth": par["max_depth"], "rr_depth": par["rr_depth"], "primitives": primitives, "accel": accel,
+            "bvh_build": bvh_build, "parallelism": f"replicas{world}",
+            "l2": "GPU arm: flushed (256 MB write) between steps"}
+
+
 def run_reference(args, rank, world) -> None:
-    """--impl reference: the CPU implementation of the path on the host cores."""
+    """--impl reference: the CPU implementation of the path (the oracle's C
+    port; rt.cpp itself renders only its own triangle scene) on all host
+    cores, on the headline Cornell frame.  The scene comes from
+    oracle/scenes/cornell_box.npz, so this arm loads no library of the CUDA
+    core."""
     if rank != 0:
         return
-    import are_gb300 as are
+    from oracle.scenes import load
 
-    scene, cam, par = are.build_config(are.CONFIG_CORNELL)
+    scene, cam, par = load("cornell_box")
     threads = os.cpu_count() or 1
     budget = float(os.environ.get("ARE_REF_STEP_SECONDS", "8"))
     vals = []
@@ -549,11 +562,11 @@ def run_reference(args, rank, world) -> None:
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(info["seconds"] * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "width": 600, "height": 600, "spp": 1024, "max_depth": 50,
-                   "l2": "n/a (CPU)"},
+        "config": workload_config(WORKLOAD, par, scene.n_prims, "linear", "host", world),
         "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{info['frames']} x {info['rows']} rows x 600 px x {info['spp']} spp of the frame per step "
-                                   f"(oracle/ C port of the estimator; rt.cpp has no quads or emission)"},
+                         "sample": f"{info['frames']} x {info['rows']} rows x {par['width']} px x {info['spp']} spp "
+                                   f"of the frame per step (oracle/ C port of the estimator; rt.cpp has no quads "
+                                   f"or emission)"},
         "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -572,6 +585,8 @@ def main() -> None:
                     help="are_render schedule (auto = megakernel)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-guiding", action="store_true", help="skip the guided-vs-plain relMSE comparison")
+    ap.add_argument("--no-extra-workloads", action="store_true",
+                    help="headline workload only (no spheres / mesh / BVH-forced Cornell lines)")
     ap.add_argument("--workload", default="cornell", choices=sorted(WORKLOADS))
     ap.add_argument("--bvh", default="host", choices=["host", "device"],
                     help="where scenes build their BVH: host binned SAH or the device LBVH")
@@ -597,40 +612,86 @@ def main() -> None:
             pg.destroy_process_group()
         return
 
-    import numpy as np
     import torch
 
     import are_gb300 as are
 
     torch.cuda.set_device(DEVICE)
-    L = are.load()
+    are.load()
     cfg_id, workload = WORKLOADS[args.workload]
-    scene_arrays, cam, par = are.build_config(cfg_id)
+    main_line = measure_render(args, args.workload, workload, cfg_id, rank, world, steps=args.steps,
+                               warmup=args.warmup, accel="auto", with_cpu=True)
+    extra = {}
+    if args.workload == "cornell" and not args.no_extra_workloads:
+        # the other single-scene workloads, each with its own e2e and CPU port, and the Cornell frame
+        # with its BVH traversed (the headline scans its 18 quads linearly)
+        extra["cornell_box_600x600_1024spp_bvh"] = measure_render(
+            args, "cornell", WORKLOADS["cornell"][1] + "_bvh", 1, rank, world, steps=3, warmup=3, accel="bvh",
+            with_cpu=False)
+        extra["random_spheres_400x225_32spp"] = measure_render(
+            args, "spheres", WORKLOADS["spheres"][1], 0, rank, world, steps=200, warmup=3, accel="auto",
+            with_cpu=True, cpu_seconds=8.0)
+        extra["mesh_2M_1920x1080_256spp"] = measure_render(
+            args, "mesh", WORKLOADS["mesh"][1], 2, rank, world, steps=2, warmup=3, accel="auto", with_cpu=True,
+            cpu_seconds=8.0, e2e_steps=2)
+
+    guiding = None
+    if rank == 0 and args.workload == "cornell" and not args.no_guiding:
+        guiding = guiding_eval()
+
+    if rank == 0:
+        line = main_line["line"]
+        if extra:
+            line["workloads"] = {k: v["summary"] for k, v in extra.items()}
+        line["guiding_equal_time"] = guiding
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def measure_render(args, key, workload, cfg_id, rank, world, steps, warmup, accel="auto", with_cpu=True,
+                   cpu_seconds=None, e2e_steps=3) -> dict:
+    """One single-scene workload through are_render: `value` (device time,
+    scene resident, image to device memory, L2 flushed between steps), e2e
+    (scene created from the host descriptor, rendered to a pinned host image,
+    destroyed, every step), the dominant kernel's roofline and, on rank 0 at
+    N = 1, the CPU port on the host cores.  Returns the full line and a
+    summary for the headline's `workloads` object."""
+    import ctypes as C
     import dataclasses
 
-    scene_arrays = dataclasses.replace(scene_arrays, bvh_build=are.BVH_DEVICE if args.bvh == "device" else are.BVH_HOST_SAH)
+    import numpy as np
+    import torch
+
+    import are_gb300 as are
+
+    L = are.load()
+    scene_arrays, cam, par = are.build_config(cfg_id)
+    scene_arrays = dataclasses.replace(scene_arrays,
+                                       bvh_build=are.BVH_DEVICE if args.bvh == "device" else are.BVH_HOST_SAH,
+                                       accel=are.ACCEL_BVH if accel == "bvh" else are.ACCEL_AUTO)
     spp = args.spp if args.spp > 0 else par["spp"]
     sched = {"auto": are.SCHEDULE_AUTO, "wavefront": are.SCHEDULE_WAVEFRONT, "megakernel": are.SCHEDULE_MEGAKERNEL}
     par = dict(par, spp=spp, pool_size=args.pool, chunk=args.chunk, schedule=sched[args.schedule])
     W, H = par["width"], par["height"]
     samples_per_step = W * H * par["spp"]
     sc = are.Scene(scene_arrays)
+    linear = accel != "bvh" and scene_arrays.n_prims <= 48
     rgb = torch.empty(W * H * 3, dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
 
     def step(seed):
         return sc.render_device(cam, dict(par, seed=seed), rgb.data_ptr())
 
-    for i in range(args.warmup):
+    for i in range(warmup):
         step(1000 + i)
     torch.cuda.synchronize()
-    if pg:
-        pg.barrier()
+    barrier(world)
     torch.cuda.synchronize()
     stats = []
     wall0 = time.perf_counter()
     with ClockSampler(SMI_INDEX) as clk:
-        for i in range(args.steps):
+        for i in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             stats.append(step(1 + i))
@@ -639,7 +700,8 @@ def main() -> None:
     barrier(world)
     dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
     torch.cuda.synchronize()
-    value = world * samples_per_step * args.steps / (dev_ms / 1e3) / 1e6
+    value = world * samples_per_step * steps / (dev_ms / 1e3) / 1e6
+    clocks = clk.summary()
 
     # kernel-level roofline over the same timed steps
     tot = {k: sum(s["kernel_ms"][k] for s in stats) for k in are.KERNELS}
@@ -652,10 +714,11 @@ def main() -> None:
     peaks = measured_peaks()
     traffic_file = REPO / "profiles" / "traffic.json"
     traffic = json.loads(traffic_file.read_text()) if traffic_file.exists() else {}
+    prof = {}
     if mega:
-        dom, t_dom, n_launch = "k_tail (megakernel)", tot["other"], args.steps
+        dom, t_dom, n_launch = "k_tail (megakernel)", tot["other"], steps
         algo_bytes = BYTES_MEGA_SAMPLE * samples + BYTES_MEGA_SEGMENT * segments
-        prof = traffic.get(f"megakernel_{args.workload}", {})
+        prof = traffic.get(f"megakernel_{key}{'_bvh' if accel == 'bvh' else ''}", {})
         per_sample = prof.get("bytes_per_sample")
         traffic_launch = round(per_sample * samples / n_launch) if per_sample is not None else None
     else:
@@ -672,76 +735,95 @@ def main() -> None:
             "kernel_ms": {k: round(v, 2) for k, v in tot.items()},
             "traffic": traffic_launch}
     if mega:
-        # what actually bounds the megakernel: instruction issue (ncu, profiles/megakernel_*.md); its DRAM
-        # traffic is a small fraction of the wavefront-equivalent bytes above
-        roof["issue_active"] = prof.get("issue_active")
-        roof["note"] = ("megakernel: path state in registers; achieved = wavefront-equivalent algorithmic bytes / "
-                        "launch time; the kernel is issue-bound (issue_active, from ncu)")
+        # What bounds the megakernel is instruction issue, not HBM: the path state stays in registers and
+        # its DRAM traffic is a small fraction of the wavefront-equivalent bytes above.  Issue roofline:
+        # warp instructions the launch executes (per segment, from the committed ncu capture of the same
+        # kernel) over what the SMs' schedulers can issue at the sampled SM clock in the launch's time.
+        ipseg = prof.get("warp_inst_per_segment")
+        mhz = clocks.get("sm_mhz") or 2070.0
+        n_sms = torch.cuda.get_device_properties(DEVICE).multi_processor_count
+        if ipseg:
+            inst = ipseg * segments
+            cap = n_sms * 4 * mhz * 1e6 * (t_dom / 1e3)
+            roof["issue"] = {"warp_inst_per_segment": ipseg, "achieved_ginst_s": round(inst / (t_dom / 1e3) / 1e9, 1),
+                             "peak_ginst_s": round(n_sms * 4 * mhz / 1e3, 1), "frac": round(inst / cap, 4),
+                             "peak_source": f"{n_sms} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)",
+                             "inst_source": prof.get("inst_source", "smsp__inst_executed.sum / segments of one "
+                                                                    "launch, ncu (profiles/traffic.json)")}
+        roof["issue_active_ncu"] = prof.get("issue_active")
+        roof["binding"] = "issue"
+        roof["note"] = ("megakernel: path state in registers; `achieved` = wavefront-equivalent algorithmic bytes / "
+                        "launch time (notional); the binding limit is instruction issue (`issue.frac`)")
 
-    # end to end through the C ABI with host buffers
-    host_rgb = np.empty(W * H * 3, np.float32)
+    # end to end through the C ABI with host buffers: scene from the host descriptor, image into a pinned
+    # host buffer, scene destroyed, every step
+    host_rgb = torch.empty(W * H * 3, dtype=torch.float32, pin_memory=True)
     e2e_times = []
     d, keep = are.desc_struct(scene_arrays)
-    import ctypes as C
-
     cam_s = are.Camera.from_dict(cam)
     build_s = []
-    for i in range(max(2, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        h = C.c_void_p()
-        are.check(L.are_scene_create(C.byref(d), C.byref(h)))
-        build_s.append(time.perf_counter() - t0)
+    for i in range(e2e_steps + 1):  # the first is a warm-up (first use of the scene kind's kernels)
+        # the call arguments are built before the clock starts: the timed region is the three C calls
         p = are.RenderParams.from_dict(dict(par, seed=77 + i))
         st = are.RenderStats()
-        are.check(L.are_render(h, C.byref(cam_s), C.byref(p), host_rgb.ctypes.data, None, C.byref(st)))
-        L.are_scene_destroy(h)
-        e2e_times.append(time.perf_counter() - t0)
+        h = C.c_void_p()
+        args_c = (C.byref(d), C.byref(h), C.byref(cam_s), C.byref(p), C.byref(st))
+        out_ptr = host_rgb.data_ptr()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc0 = L.are_scene_create(args_c[0], args_c[1])
+        t1 = time.perf_counter()
+        rc1 = L.are_render(h, args_c[2], args_c[3], out_ptr, None, args_c[4]) if rc0 == 0 else -1
+        rc2 = L.are_scene_destroy(h) if rc0 == 0 else 0
+        t2 = time.perf_counter()
+        are.check(rc0)
+        are.check(rc1)
+        are.check(rc2)
+        if i:
+            build_s.append(t1 - t0)
+            e2e_times.append(t2 - t0)
     h2d = sum(a.nbytes for a in keep if hasattr(a, "nbytes"))
     e2e = {"value": round(samples_per_step / statistics.median(e2e_times) / 1e6 * world, 3), "unit": UNIT,
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.nbytes),
-           "scene_create_ms": round(1e3 * statistics.median(build_s), 2)}
-
-    guiding = None
-    if rank == 0 and args.workload == "cornell" and not args.no_guiding:
-        guiding = guiding_eval()
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(host_rgb.numel() * 4),
+           "scene_create_ms": round(1e3 * statistics.median(build_s), 3),
+           "frame_ms": round(1e3 * statistics.median(e2e_times), 3), "host_image": "pinned"}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and with_cpu and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        r = cpu_sample(scene_arrays, cam, par, float(os.environ.get("ARE_CPU_SECONDS", "15")), threads)
+        budget = cpu_seconds or float(os.environ.get("ARE_CPU_SECONDS", "15"))
+        r = cpu_sample(scene_arrays, cam, par, budget, threads)
         cpu = {"value": round(r["value"], 4), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{r['frames']} x {r['rows']} rows x {W} px x {r['spp']} spp of the same frame "
                          f"({r['seconds']:.1f} s)"}
-        # the same port on one thread (the reference's own render() is single-threaded)
-        r1 = cpu_sample(scene_arrays, cam, par, float(os.environ.get("ARE_CPU1_SECONDS", "5")), 1)
-        cpu["one_thread"] = {"value": round(r1["value"], 4), "cores": 1,
-                             "sample": f"{r1['frames']} x {r1['rows']} rows x {W} px x {r1['spp']} spp "
-                                       f"({r1['seconds']:.1f} s)"}
+        if cpu_seconds is None:
+            # the same port on one thread (the reference's own render() is single-threaded)
+            r1 = cpu_sample(scene_arrays, cam, par, float(os.environ.get("ARE_CPU1_SECONDS", "5")), 1)
+            cpu["one_thread"] = {"value": round(r1["value"], 4), "cores": 1,
+                                 "sample": f"{r1['frames']} x {r1['rows']} rows x {W} px x {r1['spp']} spp "
+                                           f"({r1['seconds']:.1f} s)"}
 
-    if rank == 0:
-        gpu_launches = sum(sum(s["kernel_launches"].values()) for s in stats)
-        line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload, "width": W, "height": H, "spp": par["spp"], "max_depth": par["max_depth"],
-                       "rr_depth": par["rr_depth"], "primitives": scene_arrays.n_prims, "bvh_build": args.bvh,
-                       "schedule": "megakernel" if mega else "wavefront",
-                       "parallelism": f"replicas{world}",
-                       "l2": "flushed (256 MB write) between steps"},
-            "segments_per_sample": round(segments / max(1, samples), 4),
-            "tail_segments_frac": round(tail_segments / max(1, segments), 5),
-            "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
-            "wall_s": round(wall, 3),
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "clocks": clk.summary(), "gpu_launches": gpu_launches, "guiding_equal_time": guiding,
-        }
-        print(json.dumps(line), flush=True)
+    gpu_launches = sum(sum(s["kernel_launches"].values()) for s in stats)
+    config = workload_config(workload, par, scene_arrays.n_prims, "linear" if linear else "bvh", args.bvh, world)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(dev_ms / steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config, "schedule": "megakernel" if mega else "wavefront",
+        "segments_per_sample": round(segments / max(1, samples), 4),
+        "tail_segments_frac": round(tail_segments / max(1, segments), 5),
+        "rays_per_s": round(segments / (dev_ms / 1e3), 1) * world,
+        "wall_s": round(wall, 3),
+        "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+        "clocks": clocks, "gpu_launches": gpu_launches,
+    }
+    summary = {"value": line["value"], "unit": UNIT, "steps": steps, "warmup": warmup,
+               "ms_per_step": line["ms_per_step"], "config": config, "e2e": e2e, "cpu_baseline": cpu,
+               "rays_per_s": line["rays_per_s"], "segments_per_sample": line["segments_per_sample"],
+               "roofline": {k: roof.get(k) for k in ("kernel", "achieved", "frac", "issue", "traffic")},
+               "clocks": clocks, "gpu_launches": gpu_launches}
     sc.close()
-    if pg:
-        pg.destroy_process_group()
-
+    return {"line": line, "summary": summary}
 
 if __name__ == "__main__":
     main()

@@ -314,6 +314,16 @@ ARE_API int32_t are_guide_loss_history(are_guide *guide, float *out, int32_t max
 /* one Adam step (beta1 0.9, beta2 0.99) on a batch; loss before the step */
 ARE_API are_status are_guide_train(are_guide *guide, const float *samples, int64_t n, float lr, float *loss);
 
+/* Test hook for the bounded device-side waits of the tensor-core inference:
+ * each warpgroup's first wait for its tensor-core MMAs gives up after `polls`
+ * polls (-1 restores the default bound of 2^22).  A wait that gives up sets
+ * the device error bit 16, lets the work already in flight land, frees the
+ * block's tensor memory and returns, and the call reports
+ * ARE_ERR_KERNEL_TIMEOUT (inside a render, ARE_ERR_INTERNAL); with polls = 0
+ * every inference call of this guide takes that path.  No counterpart in the
+ * reference. */
+ARE_API are_status are_guide_set_wait_limit(are_guide *guide, int32_t polls);
+
 typedef struct are_guide_params {
 	float mix;            /* probability of drawing a guided vertex's direction from the network (one-sample MIS) */
 	int32_t guide_depth;  /* diffuse bounces guided per path: 0 .. 4 */
@@ -322,7 +332,8 @@ typedef struct are_guide_params {
 	                         graph launches once a quarter batch has been collected */
 	float lr;             /* Adam learning rate */
 	float weight_clip;    /* cap on a sample's weight relative to the batch mean (0 = none) */
-	int32_t reserved_[2];
+	int32_t cache_res;    /* megakernel schedule: cells per axis of the mixture cache (0 = 32, at most 128) */
+	int32_t reserved_;
 } are_guide_params;
 
 /* The path estimator (ARE_EST_PATH) with guided diffuse bounces: at each of
@@ -331,11 +342,19 @@ typedef struct are_guide_params {
  * weighted by the combined density, so the image stays unbiased whatever the
  * network has learned.  With train != 0 the network trains on the render's
  * own paths; stats->aux holds the training samples emitted, the Adam steps
- * taken, the guided vertices and the last loss.  It always runs the wavefront
- * (the network sees each bounce's rows as one batch); stats->kernel_ms holds
- * [ARE_KERNEL_INTERSECT] closest hits and input selection, [ARE_KERNEL_GENERATE]
- * network inference, [ARE_KERNEL_SHADE] guided shading, [ARE_KERNEL_OTHER]
- * the training steps. */
+ * taken, the guided vertices and the last loss.  params->schedule picks how:
+ *   MEGAKERNEL (and AUTO): the persistent path loop of are_render; the
+ *     network is evaluated on a mixture cache (cache_res^3 cells of the
+ *     scene's box x six normal directions, at the cell's centre) after every
+ *     training step, and a guided vertex samples its cell's cached mixture.
+ *     The frame runs as passes of growing size with the Adam steps and the
+ *     cache refresh between them.  stats->kernel_ms: [ARE_KERNEL_SHADE] the
+ *     path megakernel, [ARE_KERNEL_GENERATE] cache inference,
+ *     [ARE_KERNEL_OTHER] training; stats->iterations the passes.
+ *   WAVEFRONT: the network runs on every guided vertex itself (one batch per
+ *     bounce); stats->kernel_ms holds [ARE_KERNEL_INTERSECT] closest hits and
+ *     input selection, [ARE_KERNEL_GENERATE] network inference,
+ *     [ARE_KERNEL_SHADE] guided shading, [ARE_KERNEL_OTHER] the training steps. */
 ARE_API are_status are_render_guided(are_scene *scene, are_guide *guide, const are_camera *camera,
 	const are_render_params *params, const are_guide_params *guide_params, float *rgb_out, float *var_out,
 	are_render_stats *stats);

@@ -178,3 +178,19 @@ def test_ctypes_structs_match_the_header():
         subprocess.run(["gcc", "-I", str(REPO / "include"), str(c), "-o", str(exe)], check=True)
         sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert dict(zip(structs, sizes)) == structs
+
+
+def test_reference_arm_scene_files_match_the_builder(lib):
+    """The benchmark's reference arm reads its scenes from oracle/scenes/*.npz
+    (so it never loads the CUDA core); they must be the scenes the core's
+    builder makes, array for array."""
+    from oracle.scenes import load
+    for name, cfg in (("cornell_box", are.CONFIG_CORNELL), ("random_spheres", are.CONFIG_RANDOM_SPHERES)):
+        s, cam, par = load(name)
+        ref, rcam, rpar = are.build_config(cfg)
+        assert cam == rcam and par == rpar
+        for k in ("spheres", "sphere_mat", "quads", "quad_mat", "triangles", "triangle_mat"):
+            assert np.array_equal(getattr(s, k), getattr(ref, k)), (name, k)
+        assert s.materials.tobytes() == ref.materials.tobytes() and s.textures.tobytes() == ref.textures.tobytes()
+        assert (s.background, s.bg_a, s.bg_b, s.triangle_test) == (ref.background, tuple(ref.bg_a), tuple(ref.bg_b),
+                                                                    ref.triangle_test)

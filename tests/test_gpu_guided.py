@@ -22,8 +22,12 @@ def c4(res, spp, **kw):
     return s, cam, dict(par, width=res, height=res, spp=spp, **kw)
 
 
-def test_guided_is_unbiased(gpu_lib):
-    s, cam, par = c4(48, 2048, seed=3)
+SCHEDULES = [pytest.param(are.SCHEDULE_WAVEFRONT, id="wavefront"), pytest.param(are.SCHEDULE_MEGAKERNEL, id="megakernel")]
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_guided_is_unbiased(gpu_lib, schedule):
+    s, cam, par = c4(48, 2048, seed=3, schedule=schedule)
     sc = are.Scene(s)
     g = are.Guide(seed=5)
     img, var, st = sc.render_guided(g, cam, par, are.GuideParams.make(batch=1 << 12))
@@ -37,12 +41,13 @@ def test_guided_is_unbiased(gpu_lib):
     assert abs(img.mean() - ref.mean()) < 5 * se + 1e-5
 
 
-@pytest.mark.skipif(not REF.exists(), reason="FP64 reference not generated")
-def test_mix_zero_is_the_plain_estimator(gpu_lib):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_mix_zero_is_the_plain_estimator(gpu_lib, schedule):
     """With mix = 0 every guided vertex samples the cosine lobe with the same
     random numbers, and the MIS weight is exactly 1: the image is the plain
-    estimator's bit for bit, whatever the network holds."""
-    s, cam, par = c4(64, 64, seed=21)
+    estimator's bit for bit, whatever the network (or the mixture cache of the
+    megakernel schedule) holds."""
+    s, cam, par = c4(64, 64, seed=21, schedule=schedule)
     sc = are.Scene(s)
     g = are.Guide(seed=4)
     gi, gv, st = sc.render_guided(g, cam, par, are.GuideParams.make(mix=0.0, guide_depth=4, train=0))
@@ -52,11 +57,12 @@ def test_mix_zero_is_the_plain_estimator(gpu_lib):
     assert np.array_equal(gv.view(np.uint32), pv.view(np.uint32))
 
 
-def test_guided_beats_plain_at_equal_samples(gpu_lib):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_guided_beats_plain_at_equal_samples(gpu_lib, schedule):
     r = np.load(REF)
     ref = r["mean"].astype(np.float64)
     res = int(r["width"])
-    s, cam, par = c4(res, 1024, seed=7)
+    s, cam, par = c4(res, 1024, seed=7, schedule=schedule)
     sc = are.Scene(s)
     g = are.Guide(seed=1)
     gp = are.GuideParams.make(guide_depth=3, batch=1 << 14, train=2)
@@ -64,9 +70,9 @@ def test_guided_beats_plain_at_equal_samples(gpu_lib):
     for k in range(6):
         sc.render_guided(g, cam, dict(par, seed=100 + k), gp, with_var=False)
     gi, _, st = sc.render_guided(g, cam, par, are.GuideParams.make(guide_depth=3, train=0), with_var=False)
-    pi, _, _ = sc.render(cam, par, with_var=False)
+    pi, _, _ = sc.render(cam, dict(par, schedule=are.SCHEDULE_AUTO), with_var=False)
     e_g, e_p = rel_mse(gi, ref), rel_mse(pi, ref)
-    print(f"equal spp (1024): relMSE guided {e_g:.4g} plain {e_p:.4g} ratio {e_p / e_g:.2f}; "
+    print(f"equal spp (1024, schedule {schedule}): relMSE guided {e_g:.4g} plain {e_p:.4g} ratio {e_p / e_g:.2f}; "
           f"{len(g.loss_history())} Adam steps")
     assert st["train_steps"] == 0
     assert e_g < 0.85 * e_p

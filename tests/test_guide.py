@@ -154,3 +154,26 @@ def test_device_mixture_density_matches_oracle(gpu_lib, oracle):
         q = float(np.sum(pi * nrm * np.exp(kappa * (mu @ d - 1))))
         r = oracle.guide_pdf(o, d)
         assert abs(q - r) <= 0.03 * r + 1e-4, (q, r)
+
+
+@pytest.mark.gpu
+def test_bounded_wait_gives_up_and_the_next_call_succeeds(gpu_lib, oracle):
+    """The tensor-core inference's waits are bounded: with the first MMA
+    wait of each warpgroup allowed no polls, every block takes the give-up
+    path (error bit 16, work in flight drained, tensor memory freed) and the
+    call reports ARE_ERR_KERNEL_TIMEOUT; the context stays usable, so the next
+    call with the default bound returns the right answer."""
+    g = are.Guide(seed=11)
+    rng = np.random.Generator(np.random.PCG64(5))
+    feat = rng.uniform(-1, 1, (5000, 9)).astype(np.float32)
+    g.set_wait_limit(0)
+    with pytest.raises(are.AreError) as e:
+        g.forward(feat)
+    assert e.value.status == 5 and "16" in str(e.value)
+    with pytest.raises(are.AreError) as e:  # the mixture path too
+        g.mixture(feat)
+    assert e.value.status == 5
+    g.set_wait_limit(-1)
+    out = g.forward(feat)
+    ref = oracle.guide_forward(g.params, feat)
+    assert np.abs(out[:, :40] - ref[:, :40]).max() < 0.05 * max(1.0, np.abs(ref).max())
