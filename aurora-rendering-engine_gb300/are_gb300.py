@@ -187,10 +187,11 @@ KERNELS = ("intersect", "shade", "generate", "other")
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("block_size", C.c_int32), ("fetch", C.c_int32), ("leaf_size", C.c_int32), ("reserved_", C.c_int32)]
+    _fields_ = [("block_size", C.c_int32), ("fetch", C.c_int32), ("leaf_size", C.c_int32), ("bvh_width", C.c_int32)]
 
     def to_dict(self) -> dict:
-        return {"block_size": self.block_size, "fetch": self.fetch, "leaf_size": self.leaf_size}
+        return {"block_size": self.block_size, "fetch": self.fetch, "leaf_size": self.leaf_size,
+                "bvh_width": self.bvh_width}
 
 
 class TonemapParams(C.Structure):

@@ -205,14 +205,16 @@ are_status render_batch(are_scene *const *scenes, const are_camera *cams, const 
 	cudaSetDevice(device);
 	int n_sms = scenes[0]->n_sms;
 	size_t ctl_bytes = 4096 + (size_t)n * 16;
+	// the accumulators, images and control block come from the device's stream-ordered pool on the
+	// first scene's stream (the stream the batch runs on), and go back to it when the call ends
 	void *mem = nullptr;
-	are_status st = cuda_status(cudaMalloc(&mem, acc_bytes + out_bytes + ctl_bytes + sizeof(BatchScene) * n + 256),
-		"cudaMalloc(batch)");
+	are_status st = pool_alloc(scenes[0], acc_bytes + out_bytes + ctl_bytes + sizeof(BatchScene) * n + 256, &mem);
 	if (st) return st;
 	struct Free {
+		are_scene *sc;
 		void *p;
-		~Free() { cudaFree(p); }
-	} release{ mem };
+		~Free() { pool_free(sc, p); }
+	} release{ scenes[0], mem };
 	char *z = (char *)mem;
 	std::vector<float *> d_out((size_t)n);
 	for (int i = 0; i < n; ++i) {
@@ -317,18 +319,21 @@ are_status batch_autotune(const are_scene_desc *const *descs, const are_camera *
 	double best_t = 1e300;
 	std::vector<are_render_params> cal(params, params + n);
 	for (auto &p : cal) p.spp = std::max(1, std::min(p.spp, calib_spp));
-	for (int leaf : leafs) {
+	// stage 1: leaf size x block x fetch on the binary tree; stage 2: the node layout (binary or
+	// 4-wide tree) x leaf size at the best block and fetch of stage 1
+	auto calibrate = [&](int width, int leaf, const int *bs, int nb, const int *fs, int nf) -> are_status {
 		std::vector<are_scene *> sc((size_t)n, nullptr);
 		are_status st = ARE_OK;
 		for (int i = 0; i < n && !st; ++i) {
 			are_scene_desc d = *descs[i];
 			d.bvh_leaf_size = leaf;
+			d.bvh_width = width;
+			if (width == 4) d.bvh_build = ARE_BVH_HOST_SAH;  // the 4-wide collapse is made by the host build
 			st = scene_create(&d, &sc[i]);
 		}
-		for (int b : blocks)
-			for (int f : fetches) {
-				if (st) break;
-				are_batch_options o{ b, f, leaf, 0 };
+		for (int bi = 0; bi < nb && !st; ++bi)
+			for (int fi = 0; fi < nf && !st; ++fi) {
+				are_batch_options o{ bs[bi], fs[fi], leaf, width };
 				are_render_stats rs{};
 				// one warm-up, then the timed calibration launch
 				st = render_batch(sc.data(), cams, cal.data(), n, &o, nullptr, nullptr, &rs);
@@ -339,8 +344,13 @@ are_status batch_autotune(const are_scene_desc *const *descs, const are_camera *
 				}
 			}
 		for (are_scene *p : sc) delete p;
-		if (st) return st;
-	}
+		return st;
+	};
+	for (int leaf : leafs)
+		if (are_status st = calibrate(2, leaf, blocks, 3, fetches, 3)) return st;
+	const int b1 = best->block_size, f1 = best->fetch;
+	for (int leaf : leafs)
+		if (are_status st = calibrate(4, leaf, &b1, 1, &f1, 1)) return st;
 	if (best_ms) *best_ms = best_t;
 	return ARE_OK;
 }

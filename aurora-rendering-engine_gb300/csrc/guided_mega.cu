@@ -100,13 +100,10 @@ __global__ void __launch_bounds__(BLOCK) k_init_range(Wave W, int n_first, int64
 	}
 }
 
-// whether the path of (item, j) records training samples (counter 5 of its key: unused by the camera
-// ray, 0..3, and by the bounces, 8 on)
-__device__ __forceinline__ bool records(const Wave &W, const GuidedMega &G, int64_t item, int j) {
-	if (!(G.rec_prob > 0.f)) return false;
-	int pixel, sample;
-	item_coords(W, item, j, pixel, sample);
-	return uniform(path_key(W.seed, (uint32_t)pixel, (uint32_t)sample), 5) < G.rec_prob;
+// whether the path with random-number key `key` records training samples (counter 5 of its key: unused
+// by the camera ray, 0..3, and by the bounces, 8 on)
+__device__ __forceinline__ bool records(const GuidedMega &G, uint64_t key) {
+	return G.rec_prob > 0.f && uniform(key, 5) < G.rec_prob;
 }
 
 // A finished path's recorded vertices become training samples: incident radiance along the sampled
@@ -136,7 +133,7 @@ __device__ __forceinline__ void emit_samples(const GuidedMega &G, int slot, f3 L
 // false if the path ends here.
 __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMega &G, const Surface &sf, f3 d,
 	uint64_t key, int depth, int rr_depth, f3 &beta, f3 L, f3 &nd, float &rrs, bool rec, int slot, unsigned &vmask,
-	unsigned long long &gverts) {
+	unsigned long long &gverts, unsigned long long &recorded) {
 	const f3 nrm = dot(d, sf.ng) < 0.f ? sf.ng : scl(sf.ng, -1.f);
 	const float *M = G.C.mix + (size_t)cache_entry(G.C, sf.p, nrm) * GN_OUT;
 	const uint32_t cb = ctr_bounce(depth);
@@ -179,6 +176,7 @@ __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMeg
 		v[4] = make_float4(beta.x, beta.y, beta.z, 0.f);
 		v[5] = make_float4(L.x, L.y, L.z, 0.f);
 		vmask |= 1u << depth;
+		++recorded;
 	}
 	nd = w;
 	return true;
@@ -195,20 +193,18 @@ struct GuideTrack {
 // guided vertices and the training samples.  Returns true if P holds a ray to trace.
 __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, const GuidedMega &G, PathState &P,
 	GuideTrack &T, float4 h, uint32_t &err, unsigned long long &done, unsigned long long &gverts,
-	unsigned long long &emitted, float4 &sm, float4 &cm, float4 &q) {
+	unsigned long long &emitted, unsigned long long &recorded, float4 &sm, float4 &cm, float4 &q) {
 	const int leaf = __float_as_int(h.y);
 	if (leaf < 0) {
 		P.L = add(P.L, mulv(P.beta, background(S, P.d)));
 	} else {
-		int pixel, sample;
-		item_coords(W, P.item, P.j, pixel, sample);
-		const uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+		const uint64_t key = P.key;
 		const Surface sf = surface_at(S, leaf, P.o, P.d, h.x, h.z, h.w);
 		f3 nd;
 		bool cont;
 		if (P.depth < G.guide_depth && S.mats[sf.mat].type == ARE_MAT_LAMBERTIAN)
 			cont = guided_bounce(S, G, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd, T.rrs, T.rec, P.slot,
-				T.vmask, gverts);
+				T.vmask, gverts, recorded);
 		else
 			cont = scatter(S, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd, T.rrs);
 		if (cont && P.depth + 1 >= W.max_depth) cont = false;
@@ -225,7 +221,7 @@ __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, co
 	int j = P.j;
 	if (!accumulate(W, P.L, item, j, err, &W.cnt[3], sm, cm, q)) return false;
 	camera_path(W, P.slot, item, j, P);
-	T = GuideTrack{ 1.0f, 0u, records(W, G, item, j) };
+	T = GuideTrack{ 1.0f, 0u, records(G, P.key) };
 	return true;
 }
 
@@ -250,7 +246,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 		stage_nodes(S, snodes, n_snodes);
 	}
 	uint32_t err = 0;
-	unsigned long long done = 0, segments = 0, gverts = 0, emitted = 0;
+	unsigned long long done = 0, segments = 0, gverts = 0, emitted = 0, recorded = 0;
 	const float inf = __int_as_float(0x7f800000);
 	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		const unsigned i = base + threadIdx.x;
@@ -262,7 +258,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			P = load_path(W, 0, i);
 			sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
 			sm.w = cm.w = q.w = 0.f;
-			T.rec = records(W, G, P.item, P.j);
+			T.rec = records(G, P.key);
 		}
 		const int slot = P.slot;
 		if (LINEAR) {
@@ -273,7 +269,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 				if (live) {
 					++segments;
 					live = guided_step(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err,
-						done, gverts, emitted, sm, cm, q);
+						done, gverts, emitted, recorded, sm, cm, q);
 				}
 			}
 		} else {
@@ -282,7 +278,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 							  : closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
 				++segments;
 				live = guided_step(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done,
-					gverts, emitted, sm, cm, q);
+					gverts, emitted, recorded, sm, cm, q);
 			}
 		}
 		if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
@@ -292,12 +288,14 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 		segments += __shfl_down_sync(0xffffffffu, segments, o);
 		gverts += __shfl_down_sync(0xffffffffu, gverts, o);
 		emitted += __shfl_down_sync(0xffffffffu, emitted, o);
+		recorded += __shfl_down_sync(0xffffffffu, recorded, o);
 	}
 	if (lane_id() == 0) {
 		if (done) atomicAdd(&W.stat[1], done);
 		if (segments) atomicAdd(&W.stat[0], segments);
 		if (emitted) atomicAdd(&W.stat[2], emitted);
 		if (gverts) atomicAdd(&W.stat[3], gverts);
+		if (recorded) atomicAdd(&W.stat[4], recorded);
 	}
 	if (err) atomicOr(&W.cnt[4], err);
 }
@@ -364,7 +362,9 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 	GuidedMega G{};
 	G.mix = gp->mix;
 	G.guide_depth = gp->guide_depth;
-	const unsigned tcap = (unsigned)std::max(gp->batch, 256);
+	// training samples collect across passes, up to four batches, until a step takes them
+	const unsigned batch = (unsigned)std::max(gp->batch, 256);
+	const unsigned tcap = 4 * batch;
 	G.tcap = tcap;
 	for (int k = 0; k < 3; ++k) {
 		const float lo = sc->box_lo[k], ext = sc->box_hi[k] - sc->box_lo[k];
@@ -440,9 +440,13 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		cudaEventRecord(ev[5], s);
 	}
 	bool refresh_timed = !st;
-	const unsigned tmin = std::max(256u, tcap / 4);
-	double gv_per_sample = 1.5;  // guided vertices per sample, measured after each pass
-	unsigned long long prev_samples = 0, prev_gverts = 0;
+	const unsigned tmin = std::max(256u, batch / 4);  // a step needs a quarter batch: fewer make a noisy gradient
+	// measured after each pass: guided vertices per sample, and the fraction of recorded vertices whose
+	// path brought back radiance (a training sample needs a positive weight; in a scene lit mostly
+	// indirectly that is a small fraction, and the paths record with probability up to 1)
+	double gv_per_sample = 1.5, useful = 0.01;
+	unsigned held = 0;  // samples in the training buffer
+	unsigned long long prev_samples = 0, prev_gverts = 0, prev_emitted = 0, prev_recorded = 0;
 	int64_t spp_done = 0;
 	int64_t pass_spp = std::max<int64_t>(1, MG_FIRST_PASS / W.npix);
 	const int64_t max_pass_spp = std::max<int64_t>(1, MG_MAX_PASS / W.npix);
@@ -451,14 +455,14 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		const int64_t begin = spp_done * W.npix, end = (spp_done + sp) * W.npix;
 		W.n_items = end;
 		const int n_first = (int)std::min<int64_t>(P, end - begin);
-		// training samples: a random subset of the pass's paths, about 0.8 batch
-		const double expect = (double)(end - begin) * std::max(0.05, gv_per_sample);
-		G.rec_prob = gp->train ? (float)std::min(1.0, 0.8 * tcap / expect) : 0.f;
+		// training samples: a random subset of the pass's paths, sized to fill about 0.8 of the room left
+		// in the buffer with positive weights
+		const double expect = (double)(end - begin) * std::max(0.05, gv_per_sample) * std::max(1e-5, useful);
+		G.rec_prob = gp->train ? (float)std::min(1.0, 0.8 * (double)(tcap - held) / expect) : 0.f;
 		for (int k = 0; k < 8; ++k) hc[k] = 0u;
 		hc[0] = (unsigned)n_first;
 		hc[3] = (unsigned)(begin + n_first);
 		st = cuda_status(cudaMemcpyAsync(W.cnt, hc, 4 * sizeof(unsigned), cudaMemcpyHostToDevice, s), "counters");
-		if (!st) st = cuda_status(cudaMemsetAsync(G.tcount, 0, sizeof(unsigned), s), "counters");
 		if (!st) {
 			k_init_range<<<grid_of((const void *)k_init_range, sc->n_sms), BLOCK, 0, s>>>(W, n_first, begin);
 			++launches[ARE_KERNEL_OTHER];
@@ -469,7 +473,7 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 			st = cuda_status(cudaGetLastError(), "k_guided_tail launch");
 		}
 		if (!st) {
-			cudaMemcpyAsync(hc + 16, W.stat, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+			cudaMemcpyAsync(hc + 16, W.stat, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
 			cudaMemcpyAsync(hc + 8, G.tcount, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
 			st = cuda_status(cudaStreamSynchronize(s), "guided pass");
 		}
@@ -481,28 +485,35 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		refresh_timed = false;
 		const unsigned long long *hs = reinterpret_cast<const unsigned long long *>(hc + 16);
 		if (hs[1] > prev_samples) gv_per_sample = (double)(hs[3] - prev_gverts) / (double)(hs[1] - prev_samples);
-		prev_samples = hs[1], prev_gverts = hs[3];
+		if (hs[4] > prev_recorded + 64) useful = (double)(hs[2] - prev_emitted) / (double)(hs[4] - prev_recorded);
+		prev_samples = hs[1], prev_gverts = hs[3], prev_emitted = hs[2], prev_recorded = hs[4];
 		spp_done += sp;
 		pass_spp = std::min(max_pass_spp, 2 * pass_spp);
 		const unsigned have = std::min(hc[8], tcap);
+		held = have;
 		if (gp->train && have >= tmin && spp_done < p.spp) {
-			// Adam steps on what the pass collected, then the cache for the next pass
+			// `train` Adam steps on each full batch collected (or on the partial batch when there is no
+			// full one), then the cache for the next pass; the buffer starts over
 			net->weight_clip = gp->weight_clip > 0.f ? gp->weight_clip : 1e30f;
+			const unsigned nb = std::max(1u, have / batch), rows = have >= batch ? batch : have;
 			cudaEventRecord(ev[6], s);
-			for (int k = 0; k < gp->train && !st; ++k) {
-				st = net->train_step(G.tbuf, (int)have, -1.0f, gp->lr, s);
-				++train_steps;
-				launches[ARE_KERNEL_OTHER] += 7;
-			}
+			for (unsigned b = 0; b < nb && !st; ++b)
+				for (int k = 0; k < gp->train && !st; ++k) {
+					st = net->train_step(G.tbuf + (size_t)b * batch * 16, (int)rows, -1.0f, gp->lr, s);
+					++train_steps;
+					launches[ARE_KERNEL_OTHER] += 7;
+				}
 			cudaEventRecord(ev[7], s);
-			cudaMemcpyAsync(hc + 24, net->grad + GN_PARAMS, 4, cudaMemcpyDeviceToHost, s);
+			cudaMemsetAsync(G.tcount, 0, sizeof(unsigned), s);
+			held = 0;
+			cudaMemcpyAsync(hc + 28, net->grad + GN_PARAMS, 4, cudaMemcpyDeviceToHost, s);
 			cudaEventRecord(ev[4], s);
 			if (!st) st = refresh();
 			cudaEventRecord(ev[5], s);
 			refresh_timed = true;
 			if (!st) st = cuda_status(cudaStreamSynchronize(s), "guided training");
 			if (!st) {
-				net->loss_log.push_back(*reinterpret_cast<float *>(&hc[24]) / (float)have);
+				net->loss_log.push_back(*reinterpret_cast<float *>(&hc[28]) / (float)rows);
 				if (cudaEventElapsedTime(&ms, ev[6], ev[7]) == cudaSuccess) kms[ARE_KERNEL_OTHER] += ms;
 			}
 		}

@@ -51,6 +51,15 @@ __device__ __forceinline__ bool accumulate(const Wave &W, f3 L, int64_t &item, i
 		err |= ERR_NONFINITE;
 		L = f3{ 0.f, 0.f, 0.f };
 	}
+	if (W.chunk == 1) {
+		// one-sample items: the Kahan sum of one sample is the sample (sm = L, cm = 0, q = fl(L L)),
+		// published as is, without the bookkeeping
+		W.item_s[item] = make_float4(L.x, L.y, L.z, 0.f);
+		if (W.item_q) W.item_q[item] = make_float4(L.x * L.x, L.y * L.y, L.z * L.z, 0.f);
+		item = (int64_t)atomicAdd(next_item, 1u);
+		j = 0;
+		return item < W.n_items;
+	}
 	float ys[3] = { L.x - cm.x, L.y - cm.y, L.z - cm.z };
 	float ts[3] = { sm.x + ys[0], sm.y + ys[1], sm.z + ys[2] };
 	cm = make_float4((ts[0] - sm.x) - ys[0], (ts[1] - sm.y) - ys[1], (ts[2] - sm.z) - ys[2], 0.f);
@@ -85,6 +94,7 @@ struct PathState {
 	f3 o, d, beta, L;
 	int slot, depth, j;
 	uint32_t item;  // work item (fewer than 2^32, checked on the host)
+	uint64_t key;   // the sample's random-number key, path_key(seed, pixel, sample)
 };
 
 __device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i) {
@@ -95,6 +105,9 @@ __device__ __forceinline__ PathState load_path(const Wave &W, int q, unsigned i)
 	const int meta = __float_as_int(rb.w);
 	P.depth = meta & 0xff, P.j = meta >> 8;
 	P.item = (uint32_t)__float_as_int(rc.w);
+	int pixel, sample;
+	item_coords(W, P.item, P.j, pixel, sample);
+	P.key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
 	return P;
 }
 
@@ -114,6 +127,7 @@ __device__ __forceinline__ void camera_path(const Wave &W, int slot, int64_t ite
 	P.beta = f3{ 1.f, 1.f, 1.f };
 	P.L = f3{ 0.f, 0.f, 0.f };
 	P.slot = slot, P.depth = 0, P.j = j, P.item = (uint32_t)item;
+	P.key = key;
 }
 
 }  // namespace are_core

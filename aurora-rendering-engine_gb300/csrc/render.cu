@@ -158,9 +158,7 @@ __device__ __forceinline__ bool shade_step(const DevScene &S, const Wave &W, Pat
 	if (leaf < 0) {
 		P.L = add(P.L, mulv(P.beta, background(S, P.d)));
 	} else {
-		int pixel, sample;
-		item_coords(W, P.item, P.j, pixel, sample);
-		uint64_t key = path_key(W.seed, (uint32_t)pixel, (uint32_t)sample);
+		const uint64_t key = P.key;
 		Surface sf = surface_at(S, leaf, P.o, P.d, h.x, h.z, h.w);
 		f3 nd;
 		cont = scatter(S, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd);
@@ -692,21 +690,25 @@ are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, i
 	cudaStream_t s = sc->stream;
 	const float4 *d_rays = (const float4 *)rays;
 	float4 *d_hits = (float4 *)hits;
+	// the error word (and, for host pointers, the rays and hits) in one block of the device's
+	// stream-ordered pool on the scene's stream; the timing events are the scene's own
 	void *tmp = nullptr;
-	are_status st = ARE_OK;
+	const size_t io_bytes = device_ptrs ? 0 : (size_t)n * 48;
+	are_status st = pool_alloc(sc, 256 + io_bytes, &tmp);
+	if (st) return st;
+	unsigned *err_word = (unsigned *)tmp;
 	if (!device_ptrs) {
-		st = cuda_status(cudaMalloc(&tmp, (size_t)n * 48 + 256), "cudaMalloc(intersect)");
-		if (st) return st;
-		d_rays = (const float4 *)tmp;
-		d_hits = (float4 *)((char *)tmp + (size_t)n * 32);
+		d_rays = (const float4 *)((char *)tmp + 256);
+		d_hits = (float4 *)((char *)tmp + 256 + (size_t)n * 32);
 		st = cuda_status(cudaMemcpyAsync((void *)d_rays, rays, (size_t)n * 32, cudaMemcpyHostToDevice, s), "H2D rays");
 	}
-	unsigned *err_word = nullptr;
-	if (!st) st = cuda_status(cudaMallocAsync((void **)&err_word, sizeof(unsigned), s), "cudaMallocAsync");
 	if (!st) st = cuda_status(cudaMemsetAsync(err_word, 0, sizeof(unsigned), s), "memset");
-	cudaEvent_t e0, e1;
-	cudaEventCreate(&e0);
-	cudaEventCreate(&e1);
+	while (sc->render_events.size() < 2) {
+		cudaEvent_t e = nullptr;
+		cudaEventCreate(&e);
+		sc->render_events.push_back(e);
+	}
+	cudaEvent_t e0 = sc->render_events[0], e1 = sc->render_events[1];
 	if (!st) {
 		const bool linear = sc->linear;
 		int grid = grid_for(linear ? (const void *)k_intersect_batch<true> : (const void *)k_intersect_batch<false>,
@@ -724,21 +726,17 @@ are_status intersect(are_scene *sc, const float *rays, int64_t n, float *hits, i
 	if (!st) {
 		if (!device_ptrs)
 			st = cuda_status(cudaMemcpyAsync(hits, d_hits, (size_t)n * 16, cudaMemcpyDeviceToHost, s), "D2H hits");
-		cudaMemcpyAsync(&herr, err_word, sizeof herr, cudaMemcpyDeviceToHost, s);
+		cudaMemcpyAsync(sc->host_counters + 24, err_word, sizeof herr, cudaMemcpyDeviceToHost, s);
 		if (!st) st = cuda_status(cudaStreamSynchronize(s), "intersect");
+		if (!st) herr = sc->host_counters[24];
 	}
+	if (st) cudaStreamSynchronize(s);
 	if (ms) {
 		float t = 0.f;
-		cudaEventElapsedTime(&t, e0, e1);
+		if (!st) cudaEventElapsedTime(&t, e0, e1);
 		*ms = t;
 	}
-	cudaEventDestroy(e0);
-	cudaEventDestroy(e1);
-	if (err_word) cudaFreeAsync(err_word, s);
-	if (tmp) {
-		cudaStreamSynchronize(s);
-		cudaFree(tmp);
-	}
+	pool_free(sc, tmp);
 	if (!st && herr) {
 		set_error("device error word " + std::to_string(herr));
 		st = ARE_ERR_INTERNAL;

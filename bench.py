@@ -301,7 +301,7 @@ def run_batch(args, rank, world) -> None:
     t = time.perf_counter()
     best, tuned_ms = are.batch_autotune(arrays, cams, params, calib_spp=2)
     tune_s = time.perf_counter() - t
-    arrays = [dataclasses.replace(a, bvh_leaf_size=best.leaf_size) for a in arrays]
+    arrays = [dataclasses.replace(a, bvh_leaf_size=best.leaf_size, bvh_width=best.bvh_width or 0) for a in arrays]
     scenes = [are.Scene(a) for a in arrays]
     samples_per_step = sum(p["width"] * p["height"] * p["spp"] for p in params)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

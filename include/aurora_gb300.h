@@ -366,7 +366,7 @@ typedef struct are_batch_options {
 	int32_t block_size;   /* threads per block of the persistent kernel */
 	int32_t fetch;        /* work items per lane taken with each atomic on the shared queue */
 	int32_t leaf_size;    /* BVH leaf size the scenes were built with (reported by the autotuner) */
-	int32_t reserved_;
+	int32_t bvh_width;    /* BVH node layout the scenes were built with, 2 or 4 (reported by the autotuner) */
 } are_batch_options;
 
 /* No counterpart in the reference (it renders one scene).  Renders n scenes of
@@ -381,9 +381,11 @@ ARE_API are_status are_render_batch(are_scene *const *scenes, const are_camera *
 	const are_render_params *params, int32_t n, const are_batch_options *options, float *const *rgb_out,
 	double *scene_ms, are_render_stats *stats);
 
-/* Times the batch on a calibration run (spp capped at calib_spp) for every
- * BVH leaf size {2,4,8} x block size {128,256,512} x fetch {1,4,16}, building
- * the scenes from their descriptors, and returns the fastest combination. */
+/* Times the batch on a calibration run (spp capped at calib_spp), building
+ * the scenes from their descriptors: first every BVH leaf size {2,4,8} x
+ * block size {128,256,512} x fetch {1,4,16} on the binary tree, then the node
+ * layout (binary or 4-wide tree, bvh_width 2 or 4) x leaf size at the best
+ * block size and fetch; returns the fastest combination. */
 ARE_API are_status are_batch_autotune(const are_scene_desc *const *descs, const are_camera *cameras,
 	const are_render_params *params, int32_t n, int32_t calib_spp, are_batch_options *best, double *best_ms);
 

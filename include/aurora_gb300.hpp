@@ -122,6 +122,14 @@ public:
 		tris_.insert(tris_.end(), { (float)a.x, (float)a.y, (float)a.z, (float)b.x, (float)b.y, (float)b.z, (float)c.x,
 									  (float)c.y, (float)c.z });
 		tri_mat_.push_back(material);
+		if (!tri_uv_.empty()) tri_uv_.insert(tri_uv_.end(), 6, 0.0f);
+	}
+	// a triangle with per-vertex texture coordinates uv = (u0, v0, u1, v1, u2, v2) (rt.cpp:139-142 bary2uv);
+	// triangles added without them get (0, 0) at every vertex
+	void triangle(Vec3 a, Vec3 b, Vec3 c, int material, const float uv[6]) {
+		triangle(a, b, c, material);
+		tri_uv_.resize(6 * tri_mat_.size(), 0.0f);  // the earlier triangles' (0, 0)s, then this one's six
+		for (int k = 0; k < 6; ++k) tri_uv_[tri_uv_.size() - 6 + k] = uv[k];
 	}
 	void background(int kind, const float a[3], const float b[3]) {
 		bg_kind_ = kind;
@@ -140,6 +148,7 @@ public:
 		d.n_triangles = (int32_t)tri_mat_.size();
 		d.triangles = tris_.data();
 		d.triangle_mat = tri_mat_.data();
+		d.triangle_uv = tri_uv_.empty() ? nullptr : tri_uv_.data();
 		d.n_materials = (int32_t)mats_.size();
 		d.materials = mats_.data();
 		d.n_textures = (int32_t)texs_.size();
@@ -166,7 +175,7 @@ private:
 		mats_.push_back(m);
 		return (int)mats_.size() - 1;
 	}
-	std::vector<float> spheres_, quads_, tris_, texels_;
+	std::vector<float> spheres_, quads_, tris_, texels_, tri_uv_;
 	std::vector<int32_t> sphere_mat_, quad_mat_, tri_mat_;
 	std::vector<are_material> mats_;
 	std::vector<are_texture> texs_;

@@ -82,3 +82,22 @@ def same_seed_agreement(m_gpu, m_cpu, rel=1e-4):
     same = (m_gpu.view(np.uint32) == m_cpu.view(np.uint32)).mean()
     close = (np.abs(m_gpu - m_cpu) <= rel * np.maximum(1e-3, np.abs(m_cpu))).mean()
     return float(same), float(close)
+
+
+def adapted_scene() -> "are.SceneArrays":
+    """The scene tests/harness/are_adapted_scene.cpp builds from the reference
+    library's own types, as include/aurora_gb300_are.hpp converted it
+    (tests/golden/are_adapted_scene.npz), lit by a sky-gradient background."""
+    z = np.load(GOLDEN / "are_adapted_scene.npz")
+    s = are.SceneArrays()
+    s.triangles, s.triangle_uv, s.triangle_mat = z["triangles"], z["triangle_uv"], z["triangle_mat"]
+    s.materials = np.frombuffer(z["materials"].tobytes(), are.MATERIAL_DTYPE).copy()
+    s.textures = np.frombuffer(z["textures"].tobytes(), are.TEXTURE_DTYPE).copy()
+    s.texels = z["texels"]
+    s.background, s.bg_a, s.bg_b = are.BG_SKY_GRADIENT, (1.0, 1.0, 1.0), (0.5, 0.7, 1.0)
+    s.triangle_test = are.TRI_WATERTIGHT
+    return s
+
+
+ADAPTED_CAMERA = {"lookfrom": [2.0, 2.2, -3.0], "lookat": [2.0, 1.0, 2.0], "vup": [0.0, 1.0, 0.0], "vfov_deg": 60.0,
+                  "aperture": 0.0, "focus_dist": 1.0}

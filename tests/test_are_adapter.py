@@ -85,3 +85,33 @@ def test_trace_texture_definition_compiles(tmp_path):
     subprocess.run(["g++", "-std=c++20", "-Wall", "-Werror", "-c", "-I", str(REF_ROOT / "include"), "-I",
                     str(REPO / "include"), str(src), "-o", str(tmp_path / "stub.o")], check=True, capture_output=True,
                    text=True)
+
+
+def test_bound_object_set_with_materials_and_textures(tmp_path):
+    """add_object_set_bound: each triangle's are::Material and are::Texture
+    (which are::Triangle keeps private, so the caller names them) become core
+    materials and image textures — texels read through are::Texture::pixel,
+    are::Reflective(0.8) a metal of reflect_ratio 0.8, are::Diffuse
+    lambertian — and the result is the committed fixture the GPU test renders
+    (tests/golden/are_adapted_scene.npz)."""
+    from tests.golden.make_adapted_scene import build_and_run, read
+    from common import GOLDEN, are
+    out = tmp_path / "scene.bin"
+    log = build_and_run(out, tmp_path)
+    assert log.startswith("18 triangles, 5 textures, 5 materials")
+    d = read(out)
+    z = np.load(GOLDEN / "are_adapted_scene.npz")
+    for k in ("triangles", "triangle_uv", "triangle_mat", "texels"):
+        assert np.array_equal(d[k], z[k]), k
+    assert d["materials"].tobytes() == z["materials"].tobytes() and d["textures"].tobytes() == z["textures"].tobytes()
+    assert np.array_equal(d["triangle_uv"], np.tile([0, 0, 1, 0, 0, 1], (18, 1)).astype(np.float32))
+    # the floor's checker, texel (x, y) = pixel(x, y), row-major from the top
+    t0 = d["textures"][d["materials"][d["triangle_mat"][0]]["texture"]]
+    assert (t0["type"], t0["width"], t0["height"]) == (are.TEX_IMAGE, 8, 8)
+    tex = d["texels"][t0["texel_offset"]:t0["texel_offset"] + 64].reshape(8, 8, 3)
+    for y in range(8):
+        for x in range(8):
+            want = (0.1, 0.2, 0.6) if (x + y) % 2 else (0.9, 0.9, 0.9)
+            assert np.array_equal(tex[y, x], np.float32(want)), (x, y)
+    kinds = sorted((int(m["type"]), round(float(m["reflect_ratio"]), 6)) for m in d["materials"])
+    assert kinds == [(are.MAT_LAMBERTIAN, 1.0)] * 4 + [(are.MAT_METAL, 0.8)]

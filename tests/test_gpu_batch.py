@@ -49,6 +49,7 @@ def test_autotune_returns_a_valid_shape(gpu_lib):
     arrays, scenes, cams, params = small_batch(3)
     best, ms = are.batch_autotune(arrays, cams, params, calib_spp=1)
     assert best.block_size in (128, 256, 512) and best.fetch in (1, 4, 16) and best.leaf_size in (2, 4, 8)
+    assert best.bvh_width in (2, 4)
     assert ms > 0
 
 

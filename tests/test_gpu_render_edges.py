@@ -166,3 +166,22 @@ def test_image_texture_filters(gpu_lib, oracle, nthreads):
     hit = out[are.FILTER_NEAREST] < 0.999  # pixels on the quad (the sky is exactly 1)
     assert hit.mean() > 0.3
     assert not np.allclose(out[are.FILTER_NEAREST][hit], out[are.FILTER_BILINEAR][hit], atol=1e-3)
+
+
+def test_adapted_reference_scene_against_the_oracle(gpu_lib, oracle, nthreads):
+    """A scene made of the reference library's own types (are::Triangle,
+    are::Diffuse, are::Reflective, are::Texture images filled through
+    pixel()), converted by include/aurora_gb300_are.hpp (the committed
+    fixture tests/golden/are_adapted_scene.npz), rendered on the GPU and by
+    the oracle with the same random numbers: per-pixel 3-sigma agreement."""
+    from common import ADAPTED_CAMERA, adapted_scene, binomial_bound, same_seed_agreement, sigma_test
+    s = adapted_scene()
+    par = dict(width=160, height=120, spp=64, max_depth=16, seed=3, rr_depth=3, t_min=1e-4, estimator=are.EST_PATH)
+    m_gpu, v_gpu, st = are.Scene(s).render(ADAPTED_CAMERA, par)
+    m_cpu, v_cpu, _ = oracle.render(oracle.prepare(s), ADAPTED_CAMERA, par, nthreads=nthreads)
+    assert st["error_word"] == 0 and st["samples"] == 160 * 120 * 64
+    frac, _ = sigma_test(m_gpu, v_gpu, m_cpu, v_cpu)
+    same, close = same_seed_agreement(m_gpu, m_cpu)
+    assert frac <= binomial_bound(m_gpu.size), frac
+    assert close >= 0.98, close
+    assert m_gpu.mean() > 0.05  # the room is lit and visible
