@@ -292,7 +292,9 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	if (p.width <= 0 || p.height <= 0 || p.spp <= 0 || p.max_depth <= 0 || p.max_depth > 255)
 		return bad("width, height, spp must be > 0 and max_depth in [1, 255]");
 	if (!(gp->mix >= 0.f && gp->mix <= 1.f)) return bad("mix must be in [0, 1]");
-	if (gp->guide_depth < 0 || gp->guide_depth > GV) return bad("guide_depth must be in [0, 4]");
+	if (gp->guide_depth < 0 || gp->guide_depth > 255) return bad("guide_depth must be in [0, 255]");
+	if (p.schedule == ARE_SCHEDULE_WAVEFRONT && gp->guide_depth > GV)
+		return bad("guide_depth must be in [0, 4] on the wavefront schedule");
 	if (gp->train < 0 || gp->train > 16) return bad("train must be in [0, 16]");
 	if (gp->train && (gp->batch < 256 || gp->batch > (1 << 20) || !(gp->lr > 0.f))) return bad("bad training batch or lr");
 	if (!(cam->vfov_deg > 0.0f && cam->vfov_deg < 180.0f)) return bad("vfov must be in (0, 180)");

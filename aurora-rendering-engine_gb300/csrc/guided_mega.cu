@@ -138,17 +138,43 @@ __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMeg
 	const float *M = G.C.mix + (size_t)cache_entry(G.C, sf.p, nrm) * GN_OUT;
 	const uint32_t cb = ctr_bounce(depth);
 	++gverts;
-	f3 w;
-	if (uniform(key, cb + 4) < G.mix) {
-		w = packed_sample(M, uniform(key, cb + 7), uniform(key, cb + 5), uniform(key, cb + 6));
+	// Both techniques draw a direction around an axis: the cosine lobe around the normal (rt.cpp:284-289,
+	// the plain lambertian bounce's random numbers and arithmetic), or a vMF lobe around its mean; only the
+	// choice of axis and of the polar cosine differs, so the warp shares the rest (one sincos, one frame).
+	const bool guide = uniform(key, cb + 4) < G.mix;
+	f3 axis = nrm;
+	float phi_u, rs, wz = 0.f;
+	if (guide) {
+		// the first lobe whose cumulative weight exceeds u0 (the last if rounding leaves u0 above the total)
+		const float u0 = uniform(key, cb + 7), u1 = uniform(key, cb + 5);
+		int sel = GN_LOBES - 1;
+		float acc = 0.f;
+#pragma unroll
+		for (int l = 0; l < GN_LOBES - 1; ++l) {
+			acc += M[32 + 2 * l];
+			if (sel == GN_LOBES - 1 && u0 < acc) sel = l;
+		}
+		const float4 a = reinterpret_cast<const float4 *>(M)[sel];
+		// W. Jakob's stable vMF sampling: cos(theta) = 1 + log(u1 + (1 - u1) e^-2kappa) / kappa
+		wz = fminf(fmaxf(1.f + logf(u1 + (1.f - u1) * __expf(-2.f * a.w)) / a.w, -1.f), 1.f);
+		rs = sqrtf(fmaxf(0.f, 1.f - wz * wz));
+		axis = f3{ a.x, a.y, a.z };
+		phi_u = uniform(key, cb + 6);
 	} else {
-		// rt.cpp:284-289, the random numbers of the plain lambertian bounce
-		const float r1 = uniform(key, cb), r2 = uniform(key, cb + 1);
-		float s, c;
-		sincosf(6.28318530717958647692f * r1, &s, &c);
-		const float r2s = sqrtf(r2);
-		w = norm(hemi(nrm, r2s * c, r2s * s));
+		phi_u = uniform(key, cb);
+		rs = sqrtf(uniform(key, cb + 1));
 	}
+	float s, c;
+	sincosf(6.28318530717958647692f * phi_u, &s, &c);
+	const float lx = rs * c, ly = rs * s;
+	if (!guide) {
+		const float t = 1.0f - lx * lx - ly * ly;  // rt.cpp:50-55 rotateToHemisphere, as hemi()
+		wz = sqrtf(t > 0.f ? t : 0.f);
+	}
+	const f3 up = fabsf(axis.z) < 0.999f ? f3{ 0.f, 0.f, 1.f } : f3{ 1.f, 0.f, 0.f };
+	const f3 tg = norm(cross(axis, up));
+	const f3 bt = cross(axis, tg);
+	const f3 w = norm(add(add(scl(tg, lx), scl(bt, ly)), scl(axis, wz)));
 	const float cosw = dot(w, nrm);
 	if (!(cosw > 0.f)) return false;
 	const float inv_pi = 0.31830988618379067154f;
@@ -336,6 +362,10 @@ int grid_of(const void *k, int n_sms) {
 
 // pass sizes in samples: the first about 2^18, doubling to about 2^24
 constexpr int64_t MG_FIRST_PASS = 1 << 18, MG_MAX_PASS = 1 << 24;
+// Adam steps a network must have taken in its lifetime before a training render samples from it: a
+// fresh network's mixture sends paths in arbitrary directions, which costs more samples than it saves,
+// so until then such a pass guides with mix 0 (cosine sampling only) and only collects training samples
+constexpr int64_t MG_MIN_STEPS = 16;
 
 are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *cam, const are_render_params &p,
 	const are_guide_params *gp, float *rgb, float *var, are_render_stats *stats) {
@@ -455,6 +485,7 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		const int64_t begin = spp_done * W.npix, end = (spp_done + sp) * W.npix;
 		W.n_items = end;
 		const int n_first = (int)std::min<int64_t>(P, end - begin);
+		G.mix = (gp->train && net->steps < MG_MIN_STEPS) ? 0.0f : gp->mix;
 		// training samples: a random subset of the pass's paths, sized to fill about 0.8 of the room left
 		// in the buffer with positive weights
 		const double expect = (double)(end - begin) * std::max(0.05, gv_per_sample) * std::max(1e-5, useful);

@@ -206,20 +206,33 @@ def cpu_sample(scene, cam, par, budget_s: float, threads: int) -> dict:
             "segments": segments, "frames": frames}
 
 
-def guiding_eval(budget_s: float = 0.1, guide_depth: int = 3, mix: float = 0.5) -> dict | None:
+# guided estimator of the equal-time comparison: every diffuse bounce guided (guide depth = the
+# workload's max depth), one-sample MIS with the cosine lobe at mix 0.5, the megakernel schedule with a
+# 32^3 mixture cache, Adam steps on batches of 2^14 samples
+GUIDE_EVAL = {"guide_depth": 16, "mix": 0.5, "batch": 1 << 14, "train": 8, "cache_res": 32}
+GUIDE_WARM_FRAMES = 10          # earlier frames of the scene the warm network trained on
+GUIDE_WARM_SAMPLES = 40_960_000  # samples per such frame (1024 spp at 200 x 200)
+
+
+def guiding_eval(budget_s: float = 0.1) -> dict | None:
     """Equal-time relMSE of guided vs plain rendering on the occluded-light
-    Cornell box (200x200, depth 16) against the FP64 65,536-spp CPU reference
-    in tests/golden/guiding_reference_200.npz.  Each method gets the same
-    wall-clock budget for one render.  Two starts of the guided one:
-    "cold": a fresh random network that trains online inside the budget;
-    "warm": the network trained online during earlier renders of the scene
-    (as in progressive or animation rendering), training on inside the budget."""
+    Cornell box (depth 16) against the FP64 65,536-spp CPU reference
+    (tests/golden/guiding_reference_600.npz at the workload's 600 x 600 when
+    present, else guiding_reference_200.npz).  Each method gets the same
+    wall-clock budget for one render, its samples per pixel fitted on a
+    warmed call.  Two starts of the guided renderer:
+    "warm" (the headline): a network trained online while rendering
+    GUIDE_WARM_FRAMES earlier frames of the scene (as in progressive or
+    animation rendering), frozen during the timed frame;
+    "cold": a fresh random network that trains online inside the budget."""
     import numpy as np
 
     import are_gb300 as are
 
-    ref_path = REPO / "tests" / "golden" / "guiding_reference_200.npz"
-    if not ref_path.exists():
+    gold = REPO / "tests" / "golden"
+    ref_path = next((p for p in (gold / "guiding_reference_600.npz", gold / "guiding_reference_200.npz") if p.exists()),
+                    None)
+    if ref_path is None:
         return None
     r = np.load(ref_path)
     ref = r["mean"].astype(np.float64)
@@ -227,7 +240,8 @@ def guiding_eval(budget_s: float = 0.1, guide_depth: int = 3, mix: float = 0.5) 
     s, cam, par = are.build_config(are.CONFIG_CORNELL_OCCLUDED)
     par = dict(par, width=res, height=res)
     sc = are.Scene(s)
-    gp = are.GuideParams.make(guide_depth=guide_depth, mix=mix, batch=1 << 14, train=2)
+    gp = are.GuideParams.make(**GUIDE_EVAL)
+    frozen = are.GuideParams.make(**dict(GUIDE_EVAL, train=0))
 
     def relmse(img):
         return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
@@ -237,13 +251,7 @@ def guiding_eval(budget_s: float = 0.1, guide_depth: int = 3, mix: float = 0.5) 
         out = fn()
         return out, time.perf_counter() - t
 
-    def plain(spp):
-        return sc.render(cam, dict(par, spp=spp, seed=2), with_var=False)
-
-    def guided_cold(spp, seed=1):
-        return sc.render_guided(are.Guide(seed=seed), cam, dict(par, spp=spp, seed=1), gp, with_var=False)
-
-    def fit(run, spp0=512):
+    def fit(run, spp0=64):
         # seconds per sample from a warmed call (the first pays one-time set-up), then spp for the
         # budget; one correction if the budgeted render itself misses the budget by more than 10 %
         run(spp0)
@@ -255,27 +263,34 @@ def guiding_eval(budget_s: float = 0.1, guide_depth: int = 3, mix: float = 0.5) 
             res_, t = timed(lambda: run(spp))
         return res_, t, spp
 
-    (pi, _, _), t_p, spp_p = fit(plain)
+    (pi, _, _), t_p, spp_p = fit(lambda n: sc.render(cam, dict(par, spp=n, seed=2), with_var=False))
     ep = relmse(pi)
-    out = {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]), "budget_s": budget_s,
-           "guide_depth": guide_depth, "mix": mix,
-           "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 6)}}
-    (gi, _, gst), t_g, spp_g = fit(guided_cold)
-    eg = relmse(gi)
-    g = are.Guide(seed=1)  # the cold network again, trained on from here for the warm start
-    out["guided_cold"] = {"spp": spp_g, "seconds": round(t_g, 3), "relmse": round(eg, 6),
-                          "adam_steps": gst["train_steps"], "relmse_plain_over_guided": round(ep / eg, 3)}
-    # warm start: a network after seven 1024-spp renders of training
+    out = {"workload": f"cornell_occluded_{res}x{res}_depth16", "reference_spp": int(r["spp"]),
+           "reference": ref_path.name, "budget_s": budget_s, "schedule": "megakernel", **GUIDE_EVAL,
+           "plain": {"spp": spp_p, "seconds": round(t_p, 3), "relmse": round(ep, 7)}}
+    # warm start: the network trained online during earlier frames, frozen for the timed one
+    g = are.Guide(seed=1)
+    warm_spp = max(1, GUIDE_WARM_SAMPLES // (res * res))
     t = time.perf_counter()
-    for k in range(7):
-        sc.render_guided(g, cam, dict(par, spp=1024, seed=100 + k), gp, with_var=False)
+    for k in range(GUIDE_WARM_FRAMES):
+        sc.render_guided(g, cam, dict(par, spp=warm_spp, seed=100 + k), gp, with_var=False)
     t_train = time.perf_counter() - t
-    (gw, _, wst), t_w = timed(lambda: sc.render_guided(g, cam, dict(par, spp=spp_g, seed=3), gp, with_var=False))
+    (gw, _, wst), t_w, spp_w = fit(lambda n: sc.render_guided(g, cam, dict(par, spp=n, seed=3), frozen, with_var=False))
     ew = relmse(gw)
-    out["guided_warm"] = {"spp": spp_g, "seconds": round(t_w, 3), "relmse": round(ew, 6),
+    out["guided_warm"] = {"spp": spp_w, "seconds": round(t_w, 3), "relmse": round(ew, 7), "network": "frozen",
+                          "prior_frames": GUIDE_WARM_FRAMES, "prior_spp": warm_spp,
                           "prior_training_s": round(t_train, 3), "adam_steps_total": len(g.loss_history()),
                           "relmse_plain_over_guided": round(ep / ew, 3)}
-    out["relmse_plain_over_guided"] = out["guided_cold"]["relmse_plain_over_guided"]
+    # cold start: a fresh network, training inside the budget
+    (gc, _, cst), t_c, spp_c = fit(lambda n: sc.render_guided(are.Guide(seed=1), cam, dict(par, spp=n, seed=1), gp,
+                                                              with_var=False))
+    ec = relmse(gc)
+    out["guided_cold"] = {"spp": spp_c, "seconds": round(t_c, 3), "relmse": round(ec, 7),
+                          "adam_steps": cst["train_steps"], "passes": cst["iterations"],
+                          "kernel_ms": {k: round(v, 2) for k, v in cst["kernel_ms"].items()},
+                          "relmse_plain_over_guided": round(ep / ec, 3)}
+    out["relmse_plain_over_guided"] = out["guided_warm"]["relmse_plain_over_guided"]
+    out["headline_start"] = "warm"
     sc.close()
     return out
 
@@ -370,9 +385,11 @@ def run_batch(args, rank, world) -> None:
 
 def run_guided(args, rank, world) -> None:
     """--workload guided: the occluded-light Cornell frame (600x600, 1024 spp,
-    depth 16) through are_render_guided, the network training online from a
-    fresh initialisation during the warm-up frames and on through the timed
-    ones (guide depth 3, batch 2^14, two Adam steps per batch)."""
+    depth 16) through are_render_guided on the megakernel schedule (the
+    equal-time comparison's settings, GUIDE_EVAL), the network training
+    online from a fresh initialisation during the warm-up frames and on
+    through the timed ones.  --schedule wavefront runs the per-vertex network
+    (at most four guided bounces there)."""
     import torch
 
     import are_gb300 as are
@@ -381,11 +398,15 @@ def run_guided(args, rank, world) -> None:
     cfg_id, workload = WORKLOADS["guided"]
     scene_arrays, cam, par = are.build_config(cfg_id)
     spp = args.spp if args.spp > 0 else par["spp"]
-    par = dict(par, spp=spp)
+    sched = {"auto": are.SCHEDULE_AUTO, "wavefront": are.SCHEDULE_WAVEFRONT, "megakernel": are.SCHEDULE_MEGAKERNEL}
+    ge = dict(GUIDE_EVAL)
+    if args.schedule == "wavefront":
+        ge.update(guide_depth=3, train=2)
+    par = dict(par, spp=spp, schedule=sched[args.schedule])
     W, H = par["width"], par["height"]
     sc = are.Scene(scene_arrays)
     g = are.Guide(seed=1 + rank)
-    gp = are.GuideParams.make(guide_depth=3, batch=1 << 14, train=2)
+    gp = are.GuideParams.make(**ge)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for i in range(args.warmup):
         sc.render_guided(g, cam, dict(par, seed=1000 + i), gp, with_var=False)
@@ -402,33 +423,45 @@ def run_guided(args, rank, world) -> None:
     barrier(world)
     dev_ms = max_over_ranks(sum(s["device_ms"] for s in stats), world)
     samples = W * H * spp
-    # per kernel: intersect (+ network input list), inference, guided shading, training
     tot = {k: sum(s["kernel_ms"][k] for s in stats) for k in are.KERNELS}
     launches = {k: sum(s["kernel_launches"][k] for s in stats) for k in are.KERNELS}
     segs = sum(s["segments"] for s in stats)
     rows = sum(s["guided_vertices"] for s in stats)
     smp = samples * len(stats)
     peaks = measured_peaks()
-    dom = max(("intersect", "generate", "shade"), key=lambda k: tot[k])
-    if dom == "generate":  # the network on the tensor cores: its own FLOPs
-        flops = rows * GUIDE_FLOPS_PER_ROW
-        ach = flops / (tot[dom] / 1e3) / 1e12
-        roof = {"kernel": "k_guide_infer", "bound": "tensor", "achieved": round(ach, 1),
-                "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
-                "frac": round(ach / peaks["bf16_tflops_sustained"], 4), "peak_source": peaks["source"] + " (sustained)",
-                "flops_per_launch": round(flops / max(1, launches[dom]))}
+    mega = launches["intersect"] == 0
+    if mega:
+        # the guided megakernel keeps the path state in registers, as the plain one (notional bytes)
+        algo = BYTES_MEGA_SAMPLE * smp + BYTES_MEGA_SEGMENT * segs + GUIDE_BYTES_MIXTURE * rows
+        ach = algo / (tot["shade"] / 1e3) / 1e9
+        roof = {"kernel": "k_guided_tail (megakernel)", "bound": "hbm", "achieved": round(ach, 1),
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(ach / peaks["hbm_gbs"], 4),
+                "peak_source": peaks["source"], "bytes_per_launch": round(algo / max(1, launches["shade"])),
+                "binding": "issue",
+                "note": "notional wavefront-equivalent bytes plus the 192-byte cached mixture per guided vertex; "
+                        "the megakernel is issue-bound like the plain one",
+                "kernel_ms": {"path_megakernel": round(tot["shade"], 2), "cache_inference": round(tot["generate"], 2),
+                              "training": round(tot["other"], 2)}}
     else:
-        algo = {"intersect": BYTES_INTERSECT * segs + GUIDE_BYTES_IN * rows,
-                "shade": BYTES_SHADE_SEGMENT * segs + GUIDE_BYTES_MIXTURE * rows + BYTES_SHADE_SAMPLE * smp}[dom]
-        ach = algo / (tot[dom] / 1e3) / 1e9
-        roof = {"kernel": {"intersect": "k_intersect_select", "shade": "k_shade_guided"}[dom], "bound": "hbm",
-                "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": round(ach / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
-                "bytes_per_launch": round(algo / max(1, launches[dom]))}
-    roof.update({"avg_launch_us": round(tot[dom] * 1e3 / max(1, launches[dom]), 2),
-                 "kernel_ms": {"intersect_select": round(tot["intersect"], 2), "inference": round(tot["generate"], 2),
-                               "shade": round(tot["shade"], 2), "training": round(tot["other"], 2)},
-                 "traffic": None})
+        dom = max(("intersect", "generate", "shade"), key=lambda k: tot[k])
+        if dom == "generate":  # the network on the tensor cores: its own FLOPs
+            flops = rows * GUIDE_FLOPS_PER_ROW
+            ach = flops / (tot[dom] / 1e3) / 1e12
+            roof = {"kernel": "k_guide_infer", "bound": "tensor", "achieved": round(ach, 1),
+                    "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                    "frac": round(ach / peaks["bf16_tflops_sustained"], 4),
+                    "peak_source": peaks["source"] + " (sustained)", "flops_per_launch": round(flops / max(1, launches[dom]))}
+        else:
+            algo = {"intersect": BYTES_INTERSECT * segs + GUIDE_BYTES_IN * rows,
+                    "shade": BYTES_SHADE_SEGMENT * segs + GUIDE_BYTES_MIXTURE * rows + BYTES_SHADE_SAMPLE * smp}[dom]
+            ach = algo / (tot[dom] / 1e3) / 1e9
+            roof = {"kernel": {"intersect": "k_intersect_select", "shade": "k_shade_guided"}[dom], "bound": "hbm",
+                    "achieved": round(ach, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": round(ach / peaks["hbm_gbs"], 4), "peak_source": peaks["source"],
+                    "bytes_per_launch": round(algo / max(1, launches[dom]))}
+        roof["kernel_ms"] = {"intersect_select": round(tot["intersect"], 2), "inference": round(tot["generate"], 2),
+                             "shade": round(tot["shade"], 2), "training": round(tot["other"], 2)}
+    roof["traffic"] = None
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(world * samples * args.steps / (dev_ms / 1e3) / 1e6, 3), "unit": UNIT,
@@ -436,11 +469,11 @@ def run_guided(args, rank, world) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f16 network",
             "data": "synthetic",
             "config": {"workload": workload, "width": W, "height": H, "spp": spp, "max_depth": par["max_depth"],
-                       "guide_depth": 3, "mix": 0.5, "train_batch": 1 << 14, "parallelism": f"replicas{world}",
+                       **ge, "schedule": "megakernel" if mega else "wavefront", "parallelism": f"replicas{world}",
                        "l2": "flushed (256 MB write) between steps"},
             "adam_steps_per_frame": round(sum(s["train_steps"] for s in stats) / len(stats), 1),
-            "guided_vertices_per_sample": round(sum(s["guided_vertices"] for s in stats) / (samples * len(stats)), 3),
-            "segments_per_sample": round(sum(s["segments"] for s in stats) / (samples * len(stats)), 4),
+            "guided_vertices_per_sample": round(rows / smp, 3),
+            "segments_per_sample": round(segs / smp, 4),
             "roofline": roof,
             "clocks": clk.summary(),
             "gpu_launches": sum(sum(s["kernel_launches"].values()) for s in stats),

@@ -326,7 +326,8 @@ ARE_API are_status are_guide_set_wait_limit(are_guide *guide, int32_t polls);
 
 typedef struct are_guide_params {
 	float mix;            /* probability of drawing a guided vertex's direction from the network (one-sample MIS) */
-	int32_t guide_depth;  /* diffuse bounces guided per path: 0 .. 4 */
+	int32_t guide_depth;  /* diffuse bounces guided per path: 0 .. 4 on the wavefront schedule, any number on the
+	                         megakernel (training samples come from the first four either way) */
 	int32_t train;        /* Adam steps on each collected batch during the render (0 = network frozen, at most 16) */
 	int32_t batch;        /* training samples per Adam step (e.g. 2^18); a step is taken between
 	                         graph launches once a quarter batch has been collected */
