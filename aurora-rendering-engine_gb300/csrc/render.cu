@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -345,10 +346,34 @@ are_status bad(const std::string &m) {
 	return ARE_ERR_INVALID_ARGUMENT;
 }
 
+// Resident blocks per SM of each kernel, looked up once per (kernel, shared memory, device): the
+// occupancy query costs microseconds, and a frame rendered end to end (scene created, rendered,
+// destroyed) would otherwise pay it several times.
+struct OccKey {
+	const void *kernel;
+	size_t smem;
+	int device;
+};
+std::mutex g_occ_mu;
+std::vector<std::pair<OccKey, int>> g_occ;
+
 int grid_for(const void *kernel, int n_sms, size_t smem = 0) {
+	int device = 0;
+	cudaGetDevice(&device);
+	{
+		std::lock_guard<std::mutex> lk(g_occ_mu);
+		for (const auto &e : g_occ)
+			if (e.first.kernel == kernel && e.first.smem == smem && e.first.device == device) return e.second * n_sms;
+	}
 	int per_sm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem);
-	return std::max(1, per_sm) * n_sms;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem) != cudaSuccess) {
+		cudaGetLastError();
+		per_sm = 0;
+	}
+	per_sm = std::max(1, per_sm);
+	std::lock_guard<std::mutex> lk(g_occ_mu);
+	g_occ.push_back({ OccKey{ kernel, smem, device }, per_sm });
+	return per_sm * n_sms;
 }
 
 template <class T>
@@ -433,8 +458,8 @@ are_status render(are_scene *sc, const are_camera *cam, const are_render_params 
 	// state stays in registers; no queue records go through memory between bounces)
 	const bool mega = p.schedule != ARE_SCHEDULE_WAVEFRONT;
 	const bool linear = sc->linear;
-	const int g_int = intersect_grid(linear, sc->dev, sc->n_sms);
-	const int g_sh = grid_for((const void *)k_shade, sc->n_sms);
+	const int g_int = mega ? 0 : intersect_grid(linear, sc->dev, sc->n_sms);  // wavefront kernels only
+	const int g_sh = mega ? 0 : grid_for((const void *)k_shade, sc->n_sms);
 	const int g_tail = tail_grid(linear, sc->dev, sc->n_sms);
 
 	Wave W{};

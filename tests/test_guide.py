@@ -82,6 +82,8 @@ def test_device_forward_matches_oracle(gpu_lib, oracle):
     ref = oracle.guide_forward(p, s[:, :9])
     err = np.abs(out[:, :40] - ref[:, :40])
     assert np.all(np.isfinite(out))
+    print(f"\n[guide forward] max abs error {np.max(err):.3g}, mean {np.mean(err):.3g}, "
+          f"output scale {np.max(np.abs(ref)):.3g}")
     # FP16 inputs and weights, FP32 accumulation
     assert np.max(err) < 0.05 * max(1.0, np.max(np.abs(ref))), np.max(err)
     assert np.mean(err) < 0.01 * max(1.0, np.mean(np.abs(ref)))
