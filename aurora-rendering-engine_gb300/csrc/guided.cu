@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(BLOCK) k_shade_guided(DevScene S, Wave W, Guid
 						const float inv_pi = 0.31830988618379067154f;
 						float pdf = G.mix * packed_pdf(M, w) + (1.f - G.mix) * cosw * inv_pi;
 						const DevMaterial &m = S.mats[sf.mat];
-						f3 alb = tex_eval(S, m.texture, sf.u, sf.v, sf.p);
+						f3 alb = tex_albedo(S, m.texture, sf);
 						f3 L_before = L;
 						const float ratio = cosw * inv_pi / pdf;  // cosine-sampling pdf over the MIS pdf
 						beta = mulv(beta, scl(alb, ratio));

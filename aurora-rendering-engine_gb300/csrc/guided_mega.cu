@@ -180,7 +180,7 @@ __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMeg
 	const float inv_pi = 0.31830988618379067154f;
 	const float pdf = G.mix * packed_pdf(M, w) + (1.f - G.mix) * cosw * inv_pi;
 	const DevMaterial &m = S.mats[sf.mat];
-	const f3 alb = tex_eval(S, m.texture, sf.u, sf.v, sf.p);
+	const f3 alb = tex_albedo(S, m.texture, sf);
 	const float ratio = cosw * inv_pi / pdf;  // cosine-sampling pdf over the MIS pdf
 	beta = mulv(beta, scl(alb, ratio));
 	rrs = fminf(fmaxf(rrs / ratio, 1e-30f), 1e30f);

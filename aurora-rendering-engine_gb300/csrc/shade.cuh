@@ -136,12 +136,31 @@ __device__ __forceinline__ f3 background(const DevScene &S, f3 d) {
 	return ldf3(S.bg_a);
 }
 
-// Geometry at a hit: position, geometric normal, texture coordinates, material.
+// Geometry at a hit: position, geometric normal, material, and what the texture coordinates come
+// from: (u, v) as they are (quads, triangles without per-vertex uv), the sphere's normal, or the
+// barycentrics (u, v) of a triangle with per-vertex uv.  The coordinates are worked out only when a
+// texture looks them up (surface_uv): most materials are solid colours.
+enum : int32_t { UV_DIRECT = 0, UV_SPHERE = 1, UV_TRI_VERTEX = 2 };
 struct Surface {
 	f3 p, ng;
 	float u, v;
 	int32_t mat;
+	int32_t leaf, uv_kind;
 };
+
+// the texture coordinates of a surface point (sph_uv; rt.cpp:139-142 bary2uv)
+__device__ __forceinline__ void surface_uv(const DevScene &S, const Surface &sf, float &u, float &v) {
+	if (sf.uv_kind == UV_SPHERE) {
+		sph_uv(sf.ng, u, v);
+	} else if (sf.uv_kind == UV_TRI_VERTEX) {
+		const float *uv = S.tri_uv + 6 * (size_t)sf.leaf;
+		const float b0 = 1.0f - sf.u - sf.v;
+		u = uv[0] * b0 + uv[2] * sf.u + uv[4] * sf.v;
+		v = uv[1] * b0 + uv[3] * sf.u + uv[5] * sf.v;
+	} else {
+		u = sf.u, v = sf.v;
+	}
+}
 
 __device__ __forceinline__ Surface surface_at(const DevScene &S, int leaf, f3 o, f3 d, float t, float hu, float hv) {
 	Surface sf;
@@ -150,9 +169,11 @@ __device__ __forceinline__ Surface surface_at(const DevScene &S, int leaf, f3 o,
 	float4 p0 = __ldg(P);
 	sf.u = hu;
 	sf.v = hv;
+	sf.leaf = leaf;
+	sf.uv_kind = UV_DIRECT;
 	if (p0.w > 0.0f) {
 		sf.ng = scl(sub(sf.p, ld3(p0)), 1.0f / p0.w);
-		sph_uv(sf.ng, sf.u, sf.v);
+		sf.uv_kind = UV_SPHERE;
 	} else {
 		float4 p1 = __ldg(P + 1), p2 = __ldg(P + 2);
 		if (p0.w == PRIM_TAG_QUAD) {
@@ -160,17 +181,22 @@ __device__ __forceinline__ Surface surface_at(const DevScene &S, int leaf, f3 o,
 		} else {
 			f3 v0 = ld3(p0);
 			sf.ng = norm(cross(sub(ld3(p1), v0), sub(ld3(p2), v0)));
-			if (S.tri_uv) {
-				// rt.cpp:139-142 bary2uv
-				const float *uv = S.tri_uv + 6 * (size_t)leaf;
-				float b0 = 1.0f - hu - hv;
-				sf.u = uv[0] * b0 + uv[2] * hu + uv[4] * hv;
-				sf.v = uv[1] * b0 + uv[3] * hu + uv[5] * hv;
-			}
+			if (S.tri_uv) sf.uv_kind = UV_TRI_VERTEX;
 		}
 	}
 	sf.mat = __ldg(S.prim_mat + leaf);
 	return sf;
+}
+
+// tex_eval at a surface point, its texture coordinates worked out only for the textures that use them
+// (checker and image textures mapped by surface coordinates)
+__device__ __forceinline__ f3 tex_albedo(const DevScene &S, int ti, const Surface &sf) {
+	float u = 0.0f, v = 0.0f;
+	if (ti >= 0 && ti < S.n_textures) {
+		const DevTexture &t = S.texs[ti];
+		if (t.type != ARE_TEX_SOLID && t.mapping != ARE_MAP_SPHERICAL) surface_uv(S, sf, u, v);
+	}
+	return tex_eval(S, ti, u, v, sf.p);
 }
 
 // One bounce of the path estimator at depth `depth`.  Returns false if the
@@ -196,7 +222,7 @@ __device__ __forceinline__ bool scatter(const DevScene &S, const Surface &sf, f3
 		sincosf(6.28318530717958647692f * r1, &s, &c);
 		float r2s = sqrtf(r2);
 		nd = norm(hemi(n, r2s * c, r2s * s));
-		beta = mulv(beta, tex_eval(S, m.texture, sf.u, sf.v, sf.p));
+		beta = mulv(beta, tex_albedo(S, m.texture, sf));
 	} else if (m.type == ARE_MAT_METAL) {
 		f3 r = norm(reflect(d, n));
 		if (m.fuzz > 0.0f) {
@@ -210,7 +236,7 @@ __device__ __forceinline__ bool scatter(const DevScene &S, const Surface &sf, f3
 		}
 		if (!(dot(r, n) > 0.0f)) return false;
 		nd = norm(r);
-		beta = mulv(beta, tex_eval(S, m.texture, sf.u, sf.v, sf.p));
+		beta = mulv(beta, tex_albedo(S, m.texture, sf));
 	} else {
 		float ri = front ? 1.0f / m.ior : m.ior;
 		float c = -dot(d, n);
