@@ -131,6 +131,7 @@ __device__ __forceinline__ void emit_samples(const GuidedMega &G, int slot, f3 L
 // sampling; throughput times albedo cos / (pi pdf) with pdf = mix q + (1 - mix) cos / pi.  Russian
 // roulette survives with max(beta) rrs, rrs dividing out the guided bounces' pdf ratios.  Returns
 // false if the path ends here.
+template <bool TRAIN>
 __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMega &G, const Surface &sf, f3 d,
 	uint64_t key, int depth, int rr_depth, f3 &beta, f3 L, f3 &nd, float &rrs, bool rec, int slot, unsigned &vmask,
 	unsigned long long &gverts, unsigned long long &recorded) {
@@ -191,7 +192,7 @@ __device__ __forceinline__ bool guided_bounce(const DevScene &S, const GuidedMeg
 			beta = scl(beta, 1.0f / q);
 		}
 	}
-	if (rec && depth < MG_GV) {
+	if (TRAIN && rec && depth < MG_GV) {
 		float x[GN_IN];
 		guide_features(G.box, sf.p, nrm, scl(d, -1.f), x);
 		float4 *v = G.vrec + ((size_t)slot * MG_GV + depth) * 6;
@@ -217,6 +218,7 @@ struct GuideTrack {
 
 // One bounce of path P at hit h, as render.cu's shade_step with the slot's sums in registers, plus the
 // guided vertices and the training samples.  Returns true if P holds a ray to trace.
+template <bool TRAIN>
 __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, const GuidedMega &G, PathState &P,
 	GuideTrack &T, float4 h, uint32_t &err, unsigned long long &done, unsigned long long &gverts,
 	unsigned long long &emitted, unsigned long long &recorded, float4 &sm, float4 &cm, float4 &q) {
@@ -229,7 +231,7 @@ __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, co
 		f3 nd;
 		bool cont;
 		if (P.depth < G.guide_depth && S.mats[sf.mat].type == ARE_MAT_LAMBERTIAN)
-			cont = guided_bounce(S, G, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd, T.rrs, T.rec, P.slot,
+			cont = guided_bounce<TRAIN>(S, G, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd, T.rrs, T.rec, P.slot,
 				T.vmask, gverts, recorded);
 		else
 			cont = scatter(S, sf, P.d, key, P.depth, W.rr_depth, P.beta, P.L, nd, T.rrs);
@@ -241,19 +243,21 @@ __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, co
 			return true;
 		}
 	}
-	if (T.vmask) emit_samples(G, P.slot, P.L, T.vmask, emitted);
+	if (TRAIN && T.vmask) emit_samples(G, P.slot, P.L, T.vmask, emitted);
 	++done;
 	int64_t item = P.item;
 	int j = P.j;
 	if (!accumulate(W, P.L, item, j, err, &W.cnt[3], sm, cm, q)) return false;
 	camera_path(W, P.slot, item, j, P);
-	T = GuideTrack{ 1.0f, 0u, records(G, P.key) };
+	T = GuideTrack{ 1.0f, 0u, TRAIN && records(G, P.key) };
 	return true;
 }
 
 // The guided megakernel: k_tail (render.cu) with guided_step for the bounce.  One path per resident
-// thread, the slot's sums in registers; queue 0 holds the pass's first camera paths.
-template <bool LINEAR, bool WIDE = false>
+// thread, the slot's sums in registers; queue 0 holds the pass's first camera paths.  TRAIN: the
+// instantiation that records training samples (a render with a frozen network runs the one without,
+// a smaller loop).
+template <bool LINEAR, bool WIDE, bool TRAIN>
 __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
 	k_guided_tail(DevScene S, Wave W, GuidedMega G) {
 	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			P = load_path(W, 0, i);
 			sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
 			sm.w = cm.w = q.w = 0.f;
-			T.rec = records(G, P.key);
+			T.rec = TRAIN && records(G, P.key);
 		}
 		const int slot = P.slot;
 		if (LINEAR) {
@@ -294,7 +298,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 				Hit hh = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf, live, ws);
 				if (live) {
 					++segments;
-					live = guided_step(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err,
+					live = guided_step<TRAIN>(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err,
 						done, gverts, emitted, recorded, sm, cm, q);
 				}
 			}
@@ -303,7 +307,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 				Hit hh = WIDE ? closest_hit4<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x)
 							  : closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
 				++segments;
-				live = guided_step(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done,
+				live = guided_step<TRAIN>(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done,
 					gverts, emitted, recorded, sm, cm, q);
 			}
 		}
@@ -327,17 +331,29 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 }
 
 const void *guided_tail_fn(bool linear, const DevScene &S) {
-	if (linear) return (const void *)k_guided_tail<true>;
-	return S.n_nodes4 > 0 ? (const void *)k_guided_tail<false, true> : (const void *)k_guided_tail<false, false>;
+	// both instantiations of a scene kind have the same launch bounds; the training one sizes the grid
+	if (linear) return (const void *)k_guided_tail<true, false, true>;
+	return S.n_nodes4 > 0 ? (const void *)k_guided_tail<false, true, true> : (const void *)k_guided_tail<false, false, true>;
 }
 
-void launch_guided_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W, const GuidedMega &G) {
-	if (linear)
-		k_guided_tail<true><<<grid, BLOCK, 0, s>>>(S, W, G);
-	else if (S.n_nodes4 > 0)
-		k_guided_tail<false, true><<<grid, BLOCK, 0, s>>>(S, W, G);
-	else
-		k_guided_tail<false, false><<<grid, BLOCK, 0, s>>>(S, W, G);
+void launch_guided_tail(bool linear, bool train, int grid, cudaStream_t s, const DevScene &S, const Wave &W,
+	const GuidedMega &G) {
+	const bool wide = S.n_nodes4 > 0;
+	if (train) {
+		if (linear)
+			k_guided_tail<true, false, true><<<grid, BLOCK, 0, s>>>(S, W, G);
+		else if (wide)
+			k_guided_tail<false, true, true><<<grid, BLOCK, 0, s>>>(S, W, G);
+		else
+			k_guided_tail<false, false, true><<<grid, BLOCK, 0, s>>>(S, W, G);
+	} else {
+		if (linear)
+			k_guided_tail<true, false, false><<<grid, BLOCK, 0, s>>>(S, W, G);
+		else if (wide)
+			k_guided_tail<false, true, false><<<grid, BLOCK, 0, s>>>(S, W, G);
+		else
+			k_guided_tail<false, false, false><<<grid, BLOCK, 0, s>>>(S, W, G);
+	}
 }
 
 are_status bad(const std::string &m) {
@@ -498,7 +514,7 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 			k_init_range<<<grid_of((const void *)k_init_range, sc->n_sms), BLOCK, 0, s>>>(W, n_first, begin);
 			++launches[ARE_KERNEL_OTHER];
 			cudaEventRecord(ev[2], s);
-			launch_guided_tail(linear, g_tail, s, sc->dev, W, G);
+			launch_guided_tail(linear, G.rec_prob > 0.f, g_tail, s, sc->dev, W, G);
 			cudaEventRecord(ev[3], s);
 			++launches[ARE_KERNEL_SHADE];
 			st = cuda_status(cudaGetLastError(), "k_guided_tail launch");
