@@ -84,9 +84,10 @@ def test_device_forward_matches_oracle(gpu_lib, oracle):
     assert np.all(np.isfinite(out))
     print(f"\n[guide forward] max abs error {np.max(err):.3g}, mean {np.mean(err):.3g}, "
           f"output scale {np.max(np.abs(ref)):.3g}")
-    # FP16 inputs and weights, FP32 accumulation
-    assert np.max(err) < 0.05 * max(1.0, np.max(np.abs(ref))), np.max(err)
-    assert np.mean(err) < 0.01 * max(1.0, np.mean(np.abs(ref)))
+    # FP16 inputs and weights, FP32 accumulation.  Measured on GB300: max 0.0035 on outputs of scale 5.3
+    # (6.6e-4 relative), mean 4.4e-4; the bounds are about ten times those
+    assert np.max(err) < 0.007 * max(1.0, np.max(np.abs(ref))), np.max(err)
+    assert np.mean(err) < 0.0045, np.mean(err)
 
 
 @pytest.mark.gpu
