@@ -200,13 +200,14 @@ class TonemapParams(C.Structure):
 
 class GuideParams(C.Structure):
     _fields_ = [("mix", C.c_float), ("guide_depth", C.c_int32), ("train", C.c_int32), ("batch", C.c_int32),
-                ("lr", C.c_float), ("weight_clip", C.c_float), ("cache_res", C.c_int32), ("reserved_", C.c_int32)]
+                ("lr", C.c_float), ("weight_clip", C.c_float), ("cache_res", C.c_int32), ("max_steps", C.c_int32)]
 
     @staticmethod
-    def make(mix=0.5, guide_depth=2, train=1, batch=1 << 18, lr=1e-2, weight_clip=100.0, cache_res=0) -> "GuideParams":
+    def make(mix=0.5, guide_depth=2, train=1, batch=1 << 18, lr=1e-2, weight_clip=100.0, cache_res=0,
+             max_steps=0) -> "GuideParams":
         g = GuideParams()
         g.mix, g.guide_depth, g.train, g.batch, g.lr, g.weight_clip = mix, guide_depth, train, batch, lr, weight_clip
-        g.cache_res = cache_res
+        g.cache_res, g.max_steps = cache_res, max_steps
         return g
 
 

@@ -302,6 +302,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 	if (!(p.t_min >= 0.0f) || !std::isfinite(p.t_min)) return bad("t_min must be finite and >= 0");
 	if (p.schedule < ARE_SCHEDULE_AUTO || p.schedule > ARE_SCHEDULE_MEGAKERNEL) return bad("unknown schedule");
 	if (gp->cache_res < 0 || gp->cache_res > 128) return bad("cache_res must be in [0, 128]");
+	if (gp->max_steps < 0) return bad("max_steps must be >= 0");
 	cudaSetDevice(sc->device);
 	if (p.schedule != ARE_SCHEDULE_WAVEFRONT) return render_guided_mega(sc, net, cam, p, gp, rgb, var, stats);
 

@@ -505,7 +505,8 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		// training samples: a random subset of the pass's paths, sized to fill about 0.8 of the room left
 		// in the buffer with positive weights
 		const double expect = (double)(end - begin) * std::max(0.05, gv_per_sample) * std::max(1e-5, useful);
-		G.rec_prob = gp->train ? (float)std::min(1.0, 0.8 * (double)(tcap - held) / expect) : 0.f;
+		const bool training = gp->train && (gp->max_steps <= 0 || train_steps < gp->max_steps);
+		G.rec_prob = training ? (float)std::min(1.0, 0.8 * (double)(tcap - held) / expect) : 0.f;
 		for (int k = 0; k < 8; ++k) hc[k] = 0u;
 		hc[0] = (unsigned)n_first;
 		hc[3] = (unsigned)(begin + n_first);
@@ -538,14 +539,14 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 		pass_spp = std::min(max_pass_spp, 2 * pass_spp);
 		const unsigned have = std::min(hc[8], tcap);
 		held = have;
-		if (gp->train && have >= tmin && spp_done < p.spp) {
+		if (training && have >= tmin && spp_done < p.spp) {
 			// `train` Adam steps on each full batch collected (or on the partial batch when there is no
 			// full one), then the cache for the next pass; the buffer starts over
 			net->weight_clip = gp->weight_clip > 0.f ? gp->weight_clip : 1e30f;
 			const unsigned nb = std::max(1u, have / batch), rows = have >= batch ? batch : have;
 			cudaEventRecord(ev[6], s);
 			for (unsigned b = 0; b < nb && !st; ++b)
-				for (int k = 0; k < gp->train && !st; ++k) {
+				for (int k = 0; k < gp->train && !st && (gp->max_steps <= 0 || train_steps < gp->max_steps); ++k) {
 					st = net->train_step(G.tbuf + (size_t)b * batch * 16, (int)rows, -1.0f, gp->lr, s);
 					++train_steps;
 					launches[ARE_KERNEL_OTHER] += 7;

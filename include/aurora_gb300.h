@@ -334,7 +334,8 @@ typedef struct are_guide_params {
 	float lr;             /* Adam learning rate */
 	float weight_clip;    /* cap on a sample's weight relative to the batch mean (0 = none) */
 	int32_t cache_res;    /* megakernel schedule: cells per axis of the mixture cache (0 = 32, at most 128) */
-	int32_t reserved_;
+	int32_t max_steps;    /* megakernel schedule: Adam steps per render at most (0 = no limit); once they are
+	                         taken the render goes on with the network frozen, without training records */
 } are_guide_params;
 
 /* The path estimator (ARE_EST_PATH) with guided diffuse bounces: at each of

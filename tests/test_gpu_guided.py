@@ -117,3 +117,27 @@ def test_guided_vs_plain_at_equal_time(gpu_lib):
           f"ratio {e_p / e_g:.2f}; {len(g.loss_history())} Adam steps")
     assert abs(t_g - t_p) < 0.35 * budget  # the two renders took about the same time
     assert e_p / e_g >= 2.0, e_p / e_g
+
+
+@pytest.mark.parametrize("cfg,res", [(are.CONFIG_RANDOM_SPHERES, (96, 54)), (are.CONFIG_MESH, (64, 36))],
+                         ids=["spheres_binary_bvh", "mesh_4wide_bvh"])
+def test_guided_megakernel_on_bvh_scenes(gpu_lib, cfg, res):
+    """The guided megakernel's BVH instantiations (binary tree; 4-wide tree):
+    with mix 0 the image is the plain megakernel's bit for bit, and with a
+    network training online it stays within the per-pixel 3-sigma bound of a
+    plain render with another seed."""
+    s, cam, par = are.build_config(cfg)
+    par = dict(par, width=res[0], height=res[1], spp=32, seed=5, schedule=are.SCHEDULE_MEGAKERNEL)
+    sc = are.Scene(s)
+    g = are.Guide(seed=3)
+    gi, gv, st = sc.render_guided(g, cam, par, are.GuideParams.make(mix=0.0, guide_depth=8, train=0))
+    pi, pv, _ = sc.render(cam, par)
+    assert st["guided_vertices"] > 0 and st["error_word"] == 0
+    assert np.array_equal(gi.view(np.uint32), pi.view(np.uint32))
+    assert np.array_equal(gv.view(np.uint32), pv.view(np.uint32))
+    par = dict(par, spp=256)
+    img, var, st = sc.render_guided(g, cam, par, are.GuideParams.make(guide_depth=8, batch=1 << 12, train=4))
+    ref, rvar, _ = sc.render(cam, dict(par, seed=6))
+    assert st["error_word"] == 0 and np.isfinite(img).all()
+    z = np.abs(img - ref) / np.sqrt(var + rvar + 1e-12)
+    assert (z > 3).mean() < 0.02, (z > 3).mean()
