@@ -35,6 +35,7 @@
 
 #include "guide.cuh"
 #include "guide_host.h"
+#include "mega.cuh"
 #include "path.cuh"
 #include "scene.h"
 #include "wave.cuh"
@@ -278,40 +279,57 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 	uint32_t err = 0;
 	unsigned long long done = 0, segments = 0, gverts = 0, emitted = 0, recorded = 0;
 	const float inf = __int_as_float(0x7f800000);
-	for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-		const unsigned i = base + threadIdx.x;
-		bool live = i < n;
+	if constexpr (WIDE) {
 		PathState P{};
 		GuideTrack T{ 1.0f, 0u, false };
 		float4 sm{}, cm{}, q{};
-		if (live) {
-			P = load_path(W, 0, i);
-			sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
-			sm.w = cm.w = q.w = 0.f;
-			T.rec = TRAIN && records(G, P.key);
-		}
-		const int slot = P.slot;
-		if (LINEAR) {
-			// every lane stays in the loop while any lane of its warp has a path (cooperative closest hit)
-			WarpHitScratch &ws = scratch[threadIdx.x >> 5];
-			while (__any_sync(0xffffffffu, live)) {
-				Hit hh = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf, live, ws);
-				if (live) {
+		interleaved_walks<SHORT>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
+			n, gridDim.x * blockDim.x, P, err, segments,
+			[&](unsigned i) {
+				P = load_path(W, 0, i);
+				sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
+				sm.w = cm.w = q.w = 0.f;
+				T = GuideTrack{ 1.0f, 0u, TRAIN && records(G, P.key) };
+			},
+			[&](float4 h) {
+				return guided_step<TRAIN>(S, W, G, P, T, h, err, done, gverts, emitted, recorded, sm, cm, q);
+			},
+			[&]() { W.acc_s[P.slot] = sm, W.acc_c[P.slot] = cm, W.acc_q[P.slot] = q; });
+	} else {
+		for (unsigned base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+			const unsigned i = base + threadIdx.x;
+			bool live = i < n;
+			PathState P{};
+			GuideTrack T{ 1.0f, 0u, false };
+			float4 sm{}, cm{}, q{};
+			if (live) {
+				P = load_path(W, 0, i);
+				sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
+				sm.w = cm.w = q.w = 0.f;
+				T.rec = TRAIN && records(G, P.key);
+			}
+			const int slot = P.slot;
+			if (LINEAR) {
+				// every lane stays in the loop while any lane of its warp has a path (cooperative closest hit)
+				WarpHitScratch &ws = scratch[threadIdx.x >> 5];
+				while (__any_sync(0xffffffffu, live)) {
+					Hit hh = closest_hit_linear_warp(snodes, S.n_leaves, S.triangle_test, P.o, P.d, W.t_min, inf, live, ws);
+					if (live) {
+						++segments;
+						live = guided_step<TRAIN>(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v),
+							err, done, gverts, emitted, recorded, sm, cm, q);
+					}
+				}
+			} else {
+				while (live) {
+					Hit hh = closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
 					++segments;
 					live = guided_step<TRAIN>(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err,
 						done, gverts, emitted, recorded, sm, cm, q);
 				}
 			}
-		} else {
-			while (live) {
-				Hit hh = WIDE ? closest_hit4<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x)
-							  : closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
-				++segments;
-				live = guided_step<TRAIN>(S, W, G, P, T, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done,
-					gverts, emitted, recorded, sm, cm, q);
-			}
+			if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 		}
-		if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 	}
 	for (int o = 16; o > 0; o >>= 1) {
 		done += __shfl_down_sync(0xffffffffu, done, o);

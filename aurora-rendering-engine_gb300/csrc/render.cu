@@ -34,6 +34,7 @@
 
 #include "scene.h"
 #include "shade.cuh"
+#include "mega.cuh"
 #include "path.cuh"
 #include "traverse.cuh"
 #include "wave.cuh"
@@ -275,6 +276,19 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			}
 			if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 		}
+	} else if constexpr (WIDE) {
+		PathState P{};
+		float4 sm{}, cm{}, q{};
+		interleaved_walks<SHORT>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
+			n, gridDim.x * blockDim.x, P, err, segments,
+			[&](unsigned i) {
+				P = load_path(W, par, i);
+				// the slot's sums stay in registers while this thread owns the slot
+				sm = W.acc_s[P.slot], cm = W.acc_c[P.slot], q = W.acc_q[P.slot];
+				sm.w = cm.w = q.w = 0.f;
+			},
+			[&](float4 h) { return shade_step<true>(S, W, P, h, err, done, sm, cm, q); },
+			[&]() { W.acc_s[P.slot] = sm, W.acc_c[P.slot] = cm, W.acc_q[P.slot] = q; });
 	} else {
 		for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 			PathState P = load_path(W, par, i);
@@ -284,8 +298,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 			sm.w = cm.w = q.w = 0.f;
 			bool live = true;
 			while (live) {
-				Hit hh = WIDE ? closest_hit4<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x)
-							  : closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
+				Hit hh = closest_hit<SHORT>(S, snodes, n_snodes, P.o, P.d, W.t_min, inf, err, sstack + threadIdx.x);
 				++segments;
 				live = shade_step<true>(S, W, P, make_float4(hh.t, __int_as_float(hh.leaf), hh.u, hh.v), err, done, sm,
 					cm, q);

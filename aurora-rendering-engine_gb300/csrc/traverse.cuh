@@ -797,6 +797,154 @@ __device__ __forceinline__ Hit closest_hit4(const DevScene &S, const float4 *__r
 	return best;
 }
 
+// ---------------------------------------------------------------------------
+// The walk of closest_hit4 as a resumable state machine: walk4_begin sets a
+// ray up, each walk4_step visits one entry (a wide node or a leaf) and picks
+// the next, in the same order and with the same arithmetic, so the hit is the
+// same bit for bit.  A persistent kernel can then hold a lane whose walk has
+// ended (its hit waiting to be shaded) while the other lanes of its warp take
+// further steps, and can let only the lanes at a wide node (or only those at a
+// leaf) step at a time, instead of every lane waiting for the longest walk of
+// the warp at every bounce and every step running both kinds of visit.
+
+struct Walk {
+	float ix, iy, iz, ox, oy, oz;  // reciprocal direction and -origin / direction
+	Hit best;
+	int a, b;   // current entry: (reference, count: 0 = interior node, > 0 = leaf)
+	int sp;     // stack depth
+	int steps;  // entries visited
+};
+
+// the stack entries past those in shared memory
+template <int N>
+struct WalkStack {
+	int2 e[N];
+	float t[N];
+};
+
+__device__ __forceinline__ void walk_setup(f3 o, f3 d, Walk &w) {
+	w.best.t = __int_as_float(0x7f800000);
+	w.best.leaf = -1;
+	w.best.gid = 0x7fffffff;
+	w.best.u = w.best.v = 0.0f;
+	const float dx = d.x != 0.0f ? d.x : copysignf(1e-20f, d.x);
+	const float dy = d.y != 0.0f ? d.y : copysignf(1e-20f, d.y);
+	const float dz = d.z != 0.0f ? d.z : copysignf(1e-20f, d.z);
+	w.ix = __frcp_rn(dx), w.iy = __frcp_rn(dy), w.iz = __frcp_rn(dz);
+	w.ox = -o.x * w.ix, w.oy = -o.y * w.iy, w.oz = -o.z * w.iz;
+	w.sp = w.steps = 0;
+}
+
+// whether the ray of w enters box (r0, r1) between tmin and tmax
+__device__ __forceinline__ bool walk_root(const Walk &w, float4 r0, float4 r1, float tmin, float tmax) {
+	const float t0x = fmaf(r0.x, w.ix, w.ox), t1x = fmaf(r1.x, w.ix, w.ox);
+	const float t0y = fmaf(r0.y, w.iy, w.oy), t1y = fmaf(r1.y, w.iy, w.oy);
+	const float t0z = fmaf(r0.z, w.iz, w.oz), t1z = fmaf(r1.z, w.iz, w.oz);
+	const float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+	const float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax * 1.0000039f));
+	return lo <= hi;
+}
+
+// Pops the next entry that begins before the best hit; false when none is left.
+template <int SHORT, int N>
+__device__ __forceinline__ bool walk_pop(int4 *__restrict__ sstack, WalkStack<N> &st, Walk &w) {
+	while (w.sp > 0) {
+		--w.sp;
+		int2 en;
+		float te;
+		if (SHORT > 0 && w.sp < SHORT) {
+			const int4 r = sstack[w.sp * (int)blockDim.x];
+			en = make_int2(r.x, r.y);
+			te = __int_as_float(r.z);
+		} else {
+			en = st.e[w.sp - SHORT];
+			te = st.t[w.sp - SHORT];
+		}
+		if (te <= w.best.t * 1.0000039f) {
+			w.a = en.x;
+			w.b = en.y;
+			return true;
+		}
+	}
+	return false;
+}
+
+// Pushes entry e at distance te (SHORT entries in shared memory, then st).
+template <int SHORT, int N>
+__device__ __forceinline__ void walk_push(int4 *__restrict__ sstack, WalkStack<N> &st, Walk &w, int2 e, float te,
+	uint32_t &err) {
+	if (SHORT > 0 && w.sp < SHORT) {
+		sstack[w.sp++ * (int)blockDim.x] = make_int4(e.x, e.y, __float_as_int(te), 0);
+	} else if (w.sp < SHORT + N) {
+		st.e[w.sp - SHORT] = e;
+		st.t[w.sp++ - SHORT] = te;
+	} else {
+		err |= ERR_STACK_OVERFLOW;
+	}
+}
+
+// 4-wide tree (closest_hit4's walk): sets up ray (o, d); false when the ray
+// misses the root's box (the walk is over: w.best is the miss).
+__device__ __forceinline__ bool walk4_begin(const DevScene &S, f3 o, f3 d, float tmin, float tmax, Walk &w) {
+	walk_setup(o, d, w);
+	w.a = w.b = 0;
+	return walk_root(w, ldg4(S.nodes), ldg4(S.nodes + 1), tmin, tmax);
+}
+
+// 4-wide tree: visits the current entry and moves to the next; false when the walk is over.
+template <int SHORT>
+__device__ __forceinline__ bool walk4_step(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes4, f3 o,
+	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack, WalkStack<MAX_STACK4 - SHORT> &st, Walk &w) {
+	if (w.steps++ > 4 * S.n_nodes4 + 1) {  // a well-formed tree yields each entry once
+		err |= ERR_BVH_WALK;
+		return false;
+	}
+	const float inf = __int_as_float(0x7f800000);
+	if (w.b > 0) {
+		leaf_hits(S, w.a, w.b, o, d, tmin, tmax, w.best);
+	} else {
+		if ((unsigned)w.a >= (unsigned)S.n_nodes4) {
+			err |= ERR_BVH_WALK;
+			return false;
+		}
+		const bool shared = w.a < n_snodes4;
+		const float4 *__restrict__ src = shared ? snodes + 8 * w.a : S.nodes4 + 8 * (size_t)w.a;
+		const float bt = fminf(w.best.t, tmax) * 1.0000039f;
+		float l[4];
+		int2 e[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			const float4 c0 = shared ? src[2 * k] : ldg4(src + 2 * k);
+			const float4 c1 = shared ? src[2 * k + 1] : ldg4(src + 2 * k + 1);
+			const float t0x = fmaf(c0.x, w.ix, w.ox), t1x = fmaf(c1.x, w.ix, w.ox);
+			const float t0y = fmaf(c0.y, w.iy, w.oy), t1y = fmaf(c1.y, w.iy, w.oy);
+			const float t0z = fmaf(c0.z, w.iz, w.oz), t1z = fmaf(c1.z, w.iz, w.oz);
+			const float lo = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+			const float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+			e[k] = make_int2(__float_as_int(c0.w), __float_as_int(c1.w));
+			l[k] = (lo <= hi && e[k].y >= 0) ? lo : inf;
+		}
+#define ARE_CSWAP(i, j)                                           \
+	if (l[j] < l[i]) {                                            \
+		const float tl = l[i];                                    \
+		l[i] = l[j], l[j] = tl;                                   \
+		const int2 te = e[i];                                     \
+		e[i] = e[j], e[j] = te;                                   \
+	}
+		ARE_CSWAP(0, 1) ARE_CSWAP(2, 3) ARE_CSWAP(0, 2) ARE_CSWAP(1, 3) ARE_CSWAP(1, 2)
+#undef ARE_CSWAP
+#pragma unroll
+		for (int k = 3; k >= 1; --k)
+			if (l[k] < inf) walk_push<SHORT>(sstack, st, w, e[k], l[k], err);
+		if (l[0] < inf) {
+			w.a = e[0].x;
+			w.b = e[0].y;
+			return true;
+		}
+	}
+	return walk_pop<SHORT>(sstack, st, w);
+}
+
 // Stages the top of whichever tree closest_hit_any traverses.
 __device__ __forceinline__ void stage_bvh(const DevScene &S, float4 *snodes, int &n_snodes) {
 	if (S.n_nodes4 > 0)
