@@ -259,9 +259,9 @@ __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, co
 // instantiation that records training samples (a render with a frozen network runs the one without,
 // a smaller loop).
 template <bool LINEAR, bool WIDE, bool TRAIN>
-__global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
+__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
 	k_guided_tail(DevScene S, Wave W, GuidedMega G) {
-	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : WIDE ? 8 * TAIL_SMEM_NODES4 : 2 * SMEM_NODES];
 	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	constexpr int SHORT = WIDE ? TAIL_SHORT_STACK_WIDE : TAIL_SHORT_STACK;
 	__shared__ int4 sstack[LINEAR ? 1 : SHORT * BLOCK];
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else if (WIDE) {
-		stage_nodes4(S, snodes, n_snodes);
+		stage_nodes4(S, snodes, n_snodes, TAIL_SMEM_NODES4);
 	} else {
 		stage_nodes(S, snodes, n_snodes);
 	}

@@ -228,11 +228,11 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 // a scene with at most LINEAR_MAX primitives, else the BVH), each with the
 // occupancy that measured fastest for it.
 template <bool LINEAR, bool WIDE = false>
-__global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_MIN_BLOCKS_BVH)
+__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
 	k_tail(DevScene S, Wave W, int par) {
 	// linear scenes: the staged primitives and leaf boxes (6 float4 per primitive at most) and
 	// one closest-hit scratch per warp; BVH scenes: the top BVH levels
-	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : 2 * SMEM_NODES];
+	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : WIDE ? 8 * TAIL_SMEM_NODES4 : 2 * SMEM_NODES];
 	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
 	// BVH scenes: the top traversal-stack entries of every thread
 	constexpr int SHORT = WIDE ? TAIL_SHORT_STACK_WIDE : TAIL_SHORT_STACK;
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(BLOCK, LINEAR ? TAIL_MIN_BLOCKS_LINEAR : TAIL_
 		stage_prims(S, snodes);
 		__syncthreads();
 	} else if (WIDE) {
-		stage_nodes4(S, snodes, n_snodes);
+		stage_nodes4(S, snodes, n_snodes, TAIL_SMEM_NODES4);
 	} else {
 		stage_nodes(S, snodes, n_snodes);
 	}

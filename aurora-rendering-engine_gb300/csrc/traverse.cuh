@@ -673,8 +673,8 @@ __device__ __forceinline__ void leaf_hits(const DevScene &S, int a, int b, f3 o,
 
 // Stages the first SMEM_NODES4 wide nodes (breadth-first top levels) into the
 // same 32 KB buffer stage_nodes uses.
-__device__ __forceinline__ void stage_nodes4(const DevScene &S, float4 *snodes, int &n_snodes4) {
-	n_snodes4 = min(S.n_nodes4, SMEM_NODES4);
+__device__ __forceinline__ void stage_nodes4(const DevScene &S, float4 *snodes, int &n_snodes4, int max_nodes = SMEM_NODES4) {
+	n_snodes4 = min(S.n_nodes4, max_nodes);
 	for (int i = threadIdx.x; i < 8 * n_snodes4; i += blockDim.x) snodes[i] = __ldg(S.nodes4 + i);
 	__syncthreads();
 }

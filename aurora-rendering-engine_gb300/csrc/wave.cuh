@@ -13,9 +13,17 @@ namespace are_core {
 constexpr int GRAPH_ITERS = 8;  // iterations per graph launch (even)
 constexpr int BLOCK = 256;
 // resident blocks per SM requested for the tail / megakernel (registers per thread follow):
-// linear-scan scenes run best at 4 (64 registers), BVH scenes at 2 (deeper traversal state)
+// linear-scan scenes run best at 4 (64 registers); binary trees at 2 (104 registers, no spill);
+// 4-wide trees, whose walks interleave (mega.cuh), at 4 (64 registers: more warps to cover the
+// node loads of incoherent rays outweigh the spills)
 constexpr int TAIL_MIN_BLOCKS_LINEAR = 4;
 constexpr int TAIL_MIN_BLOCKS_BVH = 2;
+constexpr int TAIL_MIN_BLOCKS_WIDE = 4;
+__host__ __device__ constexpr int tail_min_blocks(bool linear, bool wide) {
+	return linear ? TAIL_MIN_BLOCKS_LINEAR : wide ? TAIL_MIN_BLOCKS_WIDE : TAIL_MIN_BLOCKS_BVH;
+}
+// wide nodes the megakernel stages in shared memory (16 KB: four blocks per SM fit with their stacks)
+constexpr int TAIL_SMEM_NODES4 = 128;
 constexpr int64_t MEGA_ITEM_BUDGET = 12ll << 30;  // bytes of per-item sums the megakernel's automatic chunk allows
 constexpr int TAIL_SHORT_STACK = 8;       // binary-tree traversal-stack entries per thread in shared memory
 constexpr int TAIL_SHORT_STACK_WIDE = 8;  // the same for the 4-wide tree
