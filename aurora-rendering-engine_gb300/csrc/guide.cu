@@ -8,9 +8,8 @@
 //                   tensor cores (tcgen05.mma, accumulators in tensor memory)
 //   k_guide_fwdbwd  fused forward + loss gradient + backward per 16-sample
 //                   tile; stores each layer's input and output gradient (FP16)
-//   k_guide_wgrad   weight gradients dW = sum_s delta_s h_s^T on the tensor
-//                   cores, K = samples, split over blocks, FP32 atomics
-//   k_guide_bgrad   bias gradients
+//   k_guide_wgrad   weight and bias gradients dW = sum_s delta_s h_s^T on the
+//                   tensor cores, K = samples, split over blocks, FP32 atomics
 //   k_guide_adam    Adam on the FP32 master weights, skipped on FP16 overflow
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -556,110 +555,139 @@ __global__ void __launch_bounds__(GT, 1) k_guide_fwdbwd(const __half *__restrict
 
 // dW[o][i] += sum over a chunk of samples of delta[s][o] * h[s][i] on the tensor
 // cores (mma.sync m16n8k16: M = outputs, N = inputs, K = samples).  The chunk
-// is staged in shared memory WG_SUB samples at a time with 16-byte loads (the
-// per-sample rows are contiguous), and each warp keeps the accumulators of its
+// is staged in shared memory WG_SUB samples at a time by asynchronous 16-byte
+// copies (the per-sample rows are contiguous) into two alternating buffers, so
+// the next sub-chunk arrives while this one is multiplied; the fragments are
+// transposing ldmatrix loads of the staged rows.  Each warp keeps the accumulators of its
 // output x input tiles in registers across the chunk, so the FP32 atomics
-// that merge blocks happen once per chunk.
-constexpr int WG_CHUNK = 256;  // samples per block
-constexpr int WG_SUB = 64;     // samples staged at a time
+// that merge blocks happen once per chunk: a block takes a chunk of
+// n / (WG_BLOCKS_PER_SM x SMs) samples, so a step's atomics do not grow with
+// its batch.  The bias gradients come out of the same products: each staged
+// input row carries a constant 1 in the column after its last input (the
+// row's padding), so the extra input tile's first column accumulates
+// sum_s delta[s][o].
+constexpr int WG_BLOCKS_PER_SM = 2;  // k_guide_wgrad blocks per SM
+constexpr int WG_SUB = 64;           // samples staged at a time
 constexpr int WG_PAD = 8;      // halves of padding per staged row (bank spread)
-constexpr size_t WG_SMEM = (size_t)WG_SUB * (GN_H + WG_PAD) * 2 + (size_t)WG_SUB * (GN_ENC + WG_PAD) * 2;
+// one staging buffer (the output gradients, then the inputs); two of them alternate
+constexpr size_t WG_D_HALVES = (size_t)WG_SUB * (GN_H + WG_PAD), WG_H_HALVES = (size_t)WG_SUB * (GN_ENC + WG_PAD);
+constexpr size_t WG_SMEM = 2 * (WG_D_HALVES + WG_H_HALVES) * 2;
 
-__device__ __forceinline__ uint32_t pack2(const __half *p, int stride) {
-	__half2 v = __halves2half2(p[0], p[stride]);
-	return h2u(v);
+// four / two 8 x 8 FP16 matrices from shared memory, transposed (ldmatrix .trans): the rows of
+// matrix j come from the addresses of lanes 8j .. 8j + 7 (16-byte aligned rows)
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const __half *p) {
+	const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+	asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+				 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+				 : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2_trans(uint32_t (&r)[2], const __half *p) {
+	const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+	asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0, %1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
 }
 
-// rows [s, s + WG_SUB) of a [samples][width] FP16 matrix -> shared memory with row stride width + WG_PAD
+// rows [s, s + WG_SUB) of a [samples][width] FP16 matrix -> shared memory with row stride width + WG_PAD,
+// as asynchronous 16-byte copies (cp.async) of the calling thread's share
 template <int WIDTH>
 __device__ __forceinline__ void stage_rows(const __half *__restrict__ src, int s, __half *dst) {
-	constexpr int V = WIDTH / 8;  // uint4 per row
+	constexpr int V = WIDTH / 8;  // 16-byte pieces per row
 	for (int e = threadIdx.x; e < WG_SUB * V; e += blockDim.x) {
 		const int r = e / V, c = e - r * V;
-		*reinterpret_cast<uint4 *>(dst + r * (WIDTH + WG_PAD) + 8 * c) =
-			*reinterpret_cast<const uint4 *>(src + (size_t)(s + r) * WIDTH + 8 * c);
+		const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + r * (WIDTH + WG_PAD) + 8 * c);
+		asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + (size_t)(s + r) * WIDTH + 8 * c)
+					 : "memory");
 	}
 }
+__device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// every copy but the most recently committed group of this thread has landed
+__device__ __forceinline__ void stage_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// sD[2], sH[2]: two staging buffers; sub-chunk i + 1 is copied in while sub-chunk i is multiplied
 template <int OUT_TILES, int IN_TILES, int DW, int HW>
 __device__ void wgrad_layer(const __half *__restrict__ D, const __half *__restrict__ H, int s0, int s1,
-	float *__restrict__ grad, int out_limit, unsigned *overflow, __half *sD, __half *sH) {
+	float *__restrict__ grad, float *__restrict__ bgrad, int out_limit, unsigned *overflow, __half *const *sD,
+	__half *const *sH) {
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	constexpr int NT = OUT_TILES * IN_TILES, PER = (NT + GT / 32 - 1) / (GT / 32);
+	// input tiles 0..IN_TILES-1 are the weights', tile IN_TILES (the padding columns: 1, 0, ..., 0) the bias's
+	constexpr int NT = OUT_TILES * (IN_TILES + 1), PER = (NT + GT / 32 - 1) / (GT / 32);
 	constexpr int DS = DW + WG_PAD, HS = HW + WG_PAD;
+	static_assert(IN_TILES * 8 == HW && WG_PAD == 8, "one padding tile after the inputs");
 	float c[PER][4];
 #pragma unroll
 	for (int k = 0; k < PER; ++k) c[k][0] = c[k][1] = c[k][2] = c[k][3] = 0.f;
-	for (int s = s0; s < s1; s += WG_SUB) {
-		__syncthreads();
-		stage_rows<DW>(D, s, sD);
-		stage_rows<HW>(H, s, sH);
-		__syncthreads();
+	__syncthreads();  // the previous layer's last products have read both buffers
+	for (int e = threadIdx.x; e < 2 * WG_SUB * WG_PAD; e += blockDim.x) {
+		const int b = e / (WG_SUB * WG_PAD), r = (e / WG_PAD) % WG_SUB, c = e % WG_PAD;
+		sH[b][r * HS + HW + c] = __float2half_rn(c == 0 ? 1.f : 0.f);
+	}
+	stage_rows<DW>(D, s0, sD[0]);
+	stage_rows<HW>(H, s0, sH[0]);
+	stage_commit();
+	int buf = 0;
+	for (int s = s0; s < s1; s += WG_SUB, buf ^= 1) {
+		if (s + WG_SUB < s1) {
+			stage_rows<DW>(D, s + WG_SUB, sD[buf ^ 1]);
+			stage_rows<HW>(H, s + WG_SUB, sH[buf ^ 1]);
+		}
+		stage_commit();
+		stage_wait_prior();
+		__syncthreads();  // sub-chunk s has landed for every thread
+		const __half *sDb = sD[buf], *sHb = sH[buf];
 #pragma unroll
 		for (int k = 0; k < PER; ++k) {
 			const int tile = warp + k * (GT / 32);
 			if (tile >= NT) break;
-			const int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
+			const int ot = tile / (IN_TILES + 1), it = tile - ot * (IN_TILES + 1);
 #pragma unroll
 			for (int kk = 0; kk < WG_SUB; kk += 16) {
-				uint32_t a[4];
-				const __half *dp = sD + (kk + 2 * t) * DS + ot * 16 + g;
-				a[0] = pack2(dp, DS);
-				a[1] = pack2(dp + 8, DS);
-				a[2] = pack2(dp + 8 * DS, DS);
-				a[3] = pack2(dp + 8 * DS + 8, DS);
-				const __half *hp = sH + (kk + 2 * t) * HS + it * 8 + g;
-				mma16816(c[k], a, pack2(hp, HS), pack2(hp + 8 * HS, HS));
+				// A (outputs x samples) and B (samples x inputs) fragments by transposing 8 x 8 loads of
+				// the sample-major staged rows: lane L addresses row L % 8 of matrix L / 8
+				uint32_t a[4], b[2];
+				ldsm_x4_trans(a, sDb + (kk + (lane & 7) + ((lane >> 4) & 1) * 8) * DS + ot * 16 + ((lane >> 3) & 1) * 8);
+				ldsm_x2_trans(b, sHb + (kk + (lane & 7) + ((lane >> 3) & 1) * 8) * HS + it * 8);
+				mma16816(c[k], a, b[0], b[1]);
 			}
 		}
+		__syncthreads();  // every product of sub-chunk s has read its buffer before the next copy into it
 	}
 #pragma unroll
 	for (int k = 0; k < PER; ++k) {
 		const int tile = warp + k * (GT / 32);
 		if (tile >= NT) break;
-		const int ot = tile / IN_TILES, it = tile - ot * IN_TILES;
+		const int ot = tile / (IN_TILES + 1), it = tile - ot * (IN_TILES + 1);
 		const int o0 = ot * 16 + g, i0 = it * 8 + 2 * t;
 		if (!(isfinite(c[k][0]) && isfinite(c[k][1]) && isfinite(c[k][2]) && isfinite(c[k][3]))) atomicOr(overflow, 1u);
+		if (it == IN_TILES) {
+			// column HW (t == 0, even half of the pair) is the bias's; the rest multiply zeros
+			if (t == 0) {
+				if (o0 < out_limit) atomicAdd(&bgrad[o0], c[k][0]);
+				if (o0 + 8 < out_limit) atomicAdd(&bgrad[o0 + 8], c[k][2]);
+			}
+			continue;
+		}
 		if (o0 < out_limit) atomicAdd(&grad[o0 * HW + i0], c[k][0]), atomicAdd(&grad[o0 * HW + i0 + 1], c[k][1]);
 		if (o0 + 8 < out_limit)
 			atomicAdd(&grad[(o0 + 8) * HW + i0], c[k][2]), atomicAdd(&grad[(o0 + 8) * HW + i0 + 1], c[k][3]);
 	}
 }
 
-__global__ void __launch_bounds__(GT) k_guide_wgrad(GuideTrainBufs B, int n, float *__restrict__ grad, unsigned *overflow) {
+// chunk: samples per block, a multiple of WG_SUB
+__global__ void __launch_bounds__(GT) k_guide_wgrad(GuideTrainBufs B, int n, int chunk, float *__restrict__ grad,
+	unsigned *overflow) {
 	// samples are padded to a multiple of 16 with zero gradients; a partial last
 	// sub-chunk reads rows up to the next multiple of WG_SUB, which the training
 	// buffers hold (ensure_train rounds their capacity up)
 	extern __shared__ __align__(16) unsigned char wsm[];
-	__half *sD = reinterpret_cast<__half *>(wsm);
-	__half *sH = sD + WG_SUB * (GN_H + WG_PAD);
-	const int s0 = blockIdx.x * WG_CHUNK, s1 = min(s0 + WG_CHUNK, n);
+	__half *const base = reinterpret_cast<__half *>(wsm);
+	__half *const sD[2] = { base, base + WG_D_HALVES };
+	__half *const sH[2] = { base + 2 * WG_D_HALVES, base + 2 * WG_D_HALVES + WG_H_HALVES };
+	const int s0 = blockIdx.x * chunk, s1 = min(s0 + chunk, n);
 	if (s0 >= s1) return;
-	wgrad_layer<4, 32, GN_H, GN_ENC>(B.d[0], B.h0, s0, s1, grad + OFF_W1, GN_H, overflow, sD, sH);
-	wgrad_layer<4, 8, GN_H, GN_H>(B.d[1], B.h[0], s0, s1, grad + OFF_W2, GN_H, overflow, sD, sH);
-	wgrad_layer<4, 8, GN_H, GN_H>(B.d[2], B.h[1], s0, s1, grad + OFF_W3, GN_H, overflow, sD, sH);
-	wgrad_layer<4, 8, GN_H, GN_H>(B.d[3], B.h[2], s0, s1, grad + OFF_W4, GN_H, overflow, sD, sH);
-	wgrad_layer<3, 8, GN_OUT, GN_H>(B.d5, B.h[3], s0, s1, grad + OFF_W5, 40, overflow, sD, sH);
-}
-
-constexpr int BG_CHUNK = 256;  // samples per block of k_guide_bgrad
-
-__global__ void k_guide_bgrad(GuideTrainBufs B, int n, float *__restrict__ grad) {
-	int col = threadIdx.x;  // 0..303
-	if (col >= 4 * GN_H + GN_OUT) return;
-	int s0 = blockIdx.x * BG_CHUNK, s1 = min(s0 + BG_CHUNK, n);
-	float acc = 0.f;
-	if (col < 4 * GN_H) {
-		int L = col / GN_H, o = col - L * GN_H;
-		for (int s = s0; s < s1; ++s) acc += __half2float(B.d[L][(size_t)s * GN_H + o]);
-		int off = L == 0 ? OFF_B1 : L == 1 ? OFF_B2 : L == 2 ? OFF_B3 : OFF_B4;
-		atomicAdd(&grad[off + o], acc);
-	} else {
-		int o = col - 4 * GN_H;
-		if (o >= 40) return;
-		for (int s = s0; s < s1; ++s) acc += __half2float(B.d5[(size_t)s * GN_OUT + o]);
-		atomicAdd(&grad[OFF_B5 + o], acc);
-	}
+	wgrad_layer<4, 32, GN_H, GN_ENC>(B.d[0], B.h0, s0, s1, grad + OFF_W1, grad + OFF_B1, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[1], B.h[0], s0, s1, grad + OFF_W2, grad + OFF_B2, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[2], B.h[1], s0, s1, grad + OFF_W3, grad + OFF_B3, GN_H, overflow, sD, sH);
+	wgrad_layer<4, 8, GN_H, GN_H>(B.d[3], B.h[2], s0, s1, grad + OFF_W4, grad + OFF_B4, GN_H, overflow, sD, sH);
+	wgrad_layer<3, 8, GN_OUT, GN_H>(B.d5, B.h[3], s0, s1, grad + OFF_W5, grad + OFF_B5, 40, overflow, sD, sH);
 }
 
 __global__ void k_guide_adam(float *__restrict__ P, float *__restrict__ m, float *__restrict__ v,
@@ -732,7 +760,8 @@ are_status GuideNet::init(uint64_t seed) {
 	if (are_status st = alloc((void **)&tc_img, TC_HALVES * sizeof(__half))) return st;
 	if (are_status st = alloc((void **)&err_word, 16)) return st;
 	if (cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_infer_smem()) != cudaSuccess ||
-		cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_train_smem()) != cudaSuccess)
+		cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_train_smem()) != cudaSuccess ||
+		cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WG_SMEM) != cudaSuccess)
 		return cuda_status(cudaGetLastError(), "cudaFuncSetAttribute(guide)");
 	// seeded He-uniform initialisation on the host (SplitMix64 stream)
 	std::vector<float> h(GN_PARAMS, 0.0f);
@@ -829,8 +858,9 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 	}
 	k_guide_fwdbwd<<<grid, GT, guide_train_smem(), s>>>(img, bias, d_samples, n, wscale, wdev, weight_clip, loss_scale,
 		bufs, grad + GN_PARAMS);
-	k_guide_wgrad<<<(np + WG_CHUNK - 1) / WG_CHUNK, GT, WG_SMEM, s>>>(bufs, np, grad, (unsigned *)(grad + GN_PARAMS + 1));
-	k_guide_bgrad<<<(np + BG_CHUNK - 1) / BG_CHUNK, 320, 0, s>>>(bufs, np, grad);
+	const int blocks = WG_BLOCKS_PER_SM * n_sms;
+	const int chunk = std::max(WG_SUB, ((np + blocks - 1) / blocks + WG_SUB - 1) / WG_SUB * WG_SUB);
+	k_guide_wgrad<<<(np + chunk - 1) / chunk, GT, WG_SMEM, s>>>(bufs, np, chunk, grad, (unsigned *)(grad + GN_PARAMS + 1));
 	return cuda_status(cudaGetLastError(), "guide gradient kernels");
 }
 
