@@ -1,13 +1,13 @@
 // guide.cu — training and inference kernels of the path-guiding network, and
 // the are_guide_* entry points.
 //
-//   k_guide_pack    FP32 master parameters -> FP16 weight image (forward rows
-//                   and transposed rows for the backward pass) + FP32 biases
-//   k_guide_pack_tc FP32 master parameters -> the tcgen05 weight image
-//   k_guide_infer   fused forward of 128-row tiles on the 5th-generation
-//                   tensor cores (tcgen05.mma, accumulators in tensor memory)
-//   k_guide_fwdbwd  fused forward + loss gradient + backward per 16-sample
-//                   tile; stores each layer's input and output gradient (FP16)
+//   k_guide_pack_tc   FP32 master parameters -> the tcgen05 weight images
+//                     (forward, and transposed for the backward pass)
+//   k_guide_infer     fused forward of 128-row tiles on the 5th-generation
+//                     tensor cores (tcgen05.mma, accumulators in tensor memory)
+//   k_guide_fwdbwd_tc the same forward plus loss gradient and backward chain
+//                     on the tensor cores; stores each layer's input and
+//                     output gradient (FP16)
 //   k_guide_wgrad   weight and bias gradients dW = sum_s delta_s h_s^T on the
 //                   tensor cores, K = samples, split over blocks, FP32 atomics
 //   k_guide_adam    Adam on the FP32 master weights, skipped on FP16 overflow
@@ -30,40 +30,19 @@ namespace {
 
 constexpr int GT = 256;  // threads per block of the MLP kernels (8 warps)
 
-__global__ void k_guide_pack(const float *__restrict__ P, __half *__restrict__ img, float *__restrict__ bias) {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < IMG_ALL + IMG_BIAS; i += gridDim.x * blockDim.x) {
-		if (i >= IMG_ALL) {
-			int b = i - IMG_ALL;
-			int off = b < 64 ? OFF_B1 + b : b < 128 ? OFF_B2 + b - 64 : b < 192 ? OFF_B3 + b - 128 : b < 256 ? OFF_B4 + b - 192 : OFF_B5 + b - 256;
-			bias[b] = (b >= 256 && b - 256 >= 40) ? 0.f : P[off];
-			continue;
-		}
-		float v = 0.f;
-		if (i < IMG_W2) {
-			int r = i / S_ENC, c = i - r * S_ENC;
-			if (c < GN_ENC) v = P[OFF_W1 + r * GN_ENC + c];
-		} else if (i < IMG_FWD) {
-			int L = i < IMG_W3 ? 2 : i < IMG_W4 ? 3 : i < IMG_W5 ? 4 : 5;
-			int base = L == 2 ? IMG_W2 : L == 3 ? IMG_W3 : L == 4 ? IMG_W4 : IMG_W5;
-			int off = L == 2 ? OFF_W2 : L == 3 ? OFF_W3 : L == 4 ? OFF_W4 : OFF_W5;
-			int r = (i - base) / S_H, c = (i - base) - r * S_H;
-			if (c < GN_H && !(L == 5 && r >= 40)) v = P[off + r * GN_H + c];
-		} else if (i < IMG_W5T) {
-			// transposed [in][out] copies of W2..W4
-			int L = i < IMG_W3T ? 2 : i < IMG_W4T ? 3 : 4;
-			int base = L == 2 ? IMG_W2T : L == 3 ? IMG_W3T : IMG_W4T;
-			int off = L == 2 ? OFF_W2 : L == 3 ? OFF_W3 : OFF_W4;
-			int in = (i - base) / S_H, o = (i - base) - in * S_H;
-			if (o < GN_H) v = P[off + o * GN_H + in];
-		} else {
-			int in = (i - IMG_W5T) / S_OUT, o = (i - IMG_W5T) - in * S_OUT;
-			if (o < 40) v = P[OFF_W5 + o * GN_H + in];
-		}
-		img[i] = __float2half_rn(v);
-	}
-}
-
 __global__ void k_guide_pack_tc(const float *__restrict__ P, __half *__restrict__ img) {
+	// the backward image (TCB_*) after the forward one
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < TCB_HALVES; i += gridDim.x * blockDim.x) {
+		int base, K, off, outs;
+		if (i < TCB_W4) base = TCB_W5, K = TCB_K5, off = OFF_W5, outs = 40;
+		else if (i < TCB_W3) base = TCB_W4, K = GN_H, off = OFF_W4, outs = GN_H;
+		else if (i < TCB_W2) base = TCB_W3, K = GN_H, off = OFF_W3, outs = GN_H;
+		else base = TCB_W2, K = GN_H, off = OFF_W2, outs = GN_H;
+		const int j = i - base, grp = j / (K * 8), rem = j - grp * (K * 8);
+		const int kc = rem >> 6, in = rem & 63;
+		const int row = grp * 8 + (in >> 3), k = kc * 8 + (in & 7);  // row: the layer's input, k: its output
+		img[TC_HALVES + i] = __float2half_rn(k < outs ? P[off + k * GN_H + row] : 0.0f);
+	}
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < TC_HALVES; i += gridDim.x * blockDim.x) {
 		// invert tc_index for the layer holding i
 		int base, K, off, boff, rows_used;
@@ -80,68 +59,6 @@ __global__ void k_guide_pack_tc(const float *__restrict__ P, __half *__restrict_
 		float v = 0.0f;
 		if (row < rows_used) v = k == one ? P[boff + row] : (k < one ? P[off + row * in_cols + k] : 0.0f);
 		img[i] = __float2half_rn(v);
-	}
-}
-
-// Copies `halves` halves and IMG_BIAS floats of the image into shared memory.
-__device__ __forceinline__ void load_image(const __half *img, const float *bias, int halves, __half *s_img,
-	float *s_bias) {
-	const uint4 *src = reinterpret_cast<const uint4 *>(img);
-	uint4 *dst = reinterpret_cast<uint4 *>(s_img);
-	for (int i = threadIdx.x; i < halves / 8; i += blockDim.x) dst[i] = src[i];
-	for (int i = threadIdx.x; i < IMG_BIAS; i += blockDim.x) s_bias[i] = bias[i];
-	__syncthreads();
-}
-
-// Forward of one 16-row tile; x0/x1 are the features of rows g and g+8.
-// Returns the output C fragments and, if keep != null, the A fragments of the
-// four hidden layers' outputs (inputs of layers 2..5).
-__device__ __forceinline__ void tile_forward(const __half *s_img, const float *s_bias, const float *x0, const float *x1,
-	float (*c5)[4], uint32_t (*keep)[4][4], __half *h0_out0, __half *h0_out1) {
-	const int t = threadIdx.x & 3;
-	float c[8][4];
-#pragma unroll
-	for (int nt = 0; nt < 8; ++nt) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.f;
-	const int g = (threadIdx.x & 31) >> 2;
-	// running (sin, cos) of the feature being encoded, rows g and g+8
-	float s0 = 0.f, k0 = 1.f, s1 = 0.f, k1 = 1.f;
-#pragma unroll
-	for (int ks = 0; ks < GN_ENC / 16; ++ks) {
-		uint32_t a[4];
-		a[0] = h2u(enc_quad(x0, ks * 8, t, s0, k0));
-		a[1] = h2u(enc_quad(x1, ks * 8, t, s1, k1));
-		a[2] = h2u(enc_quad(x0, ks * 8 + 4, t, s0, k0));
-		a[3] = h2u(enc_quad(x1, ks * 8 + 4, t, s1, k1));
-		if (h0_out0) {
-			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 2 * t) = a[0];
-			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 2 * t) = a[1];
-			*reinterpret_cast<uint32_t *>(h0_out0 + ks * 16 + 8 + 2 * t) = a[2];
-			*reinterpret_cast<uint32_t *>(h0_out1 + ks * 16 + 8 + 2 * t) = a[3];
-		}
-		if (ks * 8 >= 116) continue;  // pairs 116.. of the encoding are zero
-#pragma unroll
-		for (int nt = 0; nt < 8; ++nt) {
-			const __half *row = s_img + IMG_W1 + (nt * 8 + g) * S_ENC + ks * 16 + 2 * t;
-			mma16816(c[nt], a, *reinterpret_cast<const uint32_t *>(row), *reinterpret_cast<const uint32_t *>(row + 8));
-		}
-	}
-	uint32_t a[4][4];
-	relu_to_a(c, s_bias + 0, a);
-	if (keep) memcpy(keep[0], a, sizeof a);
-	tile_layer<4, 8>(a, s_img + IMG_W2, S_H, c);
-	relu_to_a(c, s_bias + 64, a);
-	if (keep) memcpy(keep[1], a, sizeof a);
-	tile_layer<4, 8>(a, s_img + IMG_W3, S_H, c);
-	relu_to_a(c, s_bias + 128, a);
-	if (keep) memcpy(keep[2], a, sizeof a);
-	tile_layer<4, 8>(a, s_img + IMG_W4, S_H, c);
-	relu_to_a(c, s_bias + 192, a);
-	if (keep) memcpy(keep[3], a, sizeof a);
-	tile_layer<4, 6>(a, s_img + IMG_W5, S_H, c5);
-#pragma unroll
-	for (int nt = 0; nt < 6; ++nt) {
-		float b0 = s_bias[256 + nt * 8 + 2 * t], b1 = s_bias[256 + nt * 8 + 2 * t + 1];
-		c5[nt][0] += b0, c5[nt][1] += b1, c5[nt][2] += b0, c5[nt][3] += b1;
 	}
 }
 
@@ -435,122 +352,243 @@ __device__ float sample_out_grad(const float *o, f3 w, float wt, float *g) {
 	return -wt * logf(q);
 }
 
-// backward of a hidden layer: C = (delta A) (16 x K_out) x W^T-image, masked
-// by the forward activations `h` (A fragments, h > 0), returned as A fragments.
-template <int KSTEPS>
-__device__ __forceinline__ void back_layer(const uint32_t (*da)[4], const __half *WT, int stride, const uint32_t (*h)[4],
-	uint32_t (*out)[4], float scale_clip) {
-	float c[8][4];
-	tile_layer<KSTEPS, 8>(da, WT, stride, c);
+// ---- forward + backward of a training batch on the 5th-generation tensor cores
+//
+// k_guide_fwdbwd_tc runs k_guide_infer's forward on 128-row tiles (thread t of
+// a warpgroup owns row t) and then, per row: stores its encoding and its four
+// hidden activations (FP16, for k_guide_wgrad; the encoding with 0 in the
+// bias column, as the master layout has it) and keeps their ReLU masks as bits;
+// computes d(-log q)/d(outputs) times the sample's weight and the loss scale
+// (sample_out_grad, clipped, FP16) and stores it; then the backward chain on
+// the tensor cores: that gradient tile times layer 5's transposed weights
+// (K = 48) gives the gradient at h4, which is masked by h4 > 0, clipped,
+// rounded to FP16, stored and multiplied by W4^T, and so on down to the
+// gradient at h1.  The same numbers as k_guide_fwdbwd up to the order of FP32
+// sums and the encoding's last bits.  Waits are bounded as in k_guide_infer;
+// a warpgroup that gives up sets ERR_TENSOR_TIMEOUT and the step's overflow
+// flag, so the Adam step that follows is skipped.
+constexpr size_t TT_OFF_A = (size_t)(TC_HALVES + TCB_HALVES) * 2;
+constexpr size_t TT_OFF_BAR = TT_OFF_A + (size_t)TC_WG * TC_A_BYTES;
+constexpr size_t TT_SMEM = TT_OFF_BAR + 128;
+static_assert(TT_OFF_A % 16 == 0 && TT_OFF_BAR % 8 == 0, "bulk copy / mbarrier alignment");
+static_assert(TT_SMEM <= 227 * 1024, "shared memory of one block");
+static_assert(TCB_K5 % 16 == 0 && GN_H % 16 == 0, "backward K in 16-element steps");
+
+// the 64 accumulators of row lt at columns [col, col + 64) -> FP16 pairs (ReLU'd when relu, else
+// multiplied by the mask bits and clipped), written to the row's input tile (8 chunks) and,
+// when g is not null, to g[0..7] (the row's 128 bytes in global memory); relu also returns the
+// mask bits (value > 0) of the 64 results
+__device__ __forceinline__ uint64_t tt_epilogue(uint32_t taddr, unsigned char *hrow, uint4 *g, bool relu,
+	uint64_t mask, float clip) {
+	uint64_t bits = 0;
 #pragma unroll
-	for (int ks = 0; ks < 4; ++ks) {
+	for (int h = 0; h < 2; ++h) {
+		uint32_t r[2][16];
+		tmem_ld16(taddr + 32u * h, r[0]);
+		tmem_ld16(taddr + 32u * h + 16u, r[1]);
+		tmem_ld_wait();
 #pragma unroll
-		for (int hh = 0; hh < 2; ++hh) {
-			int nt = 2 * ks + hh;
-			__half2 hr0 = u2h(h[ks][2 * hh]), hr1 = u2h(h[ks][2 * hh + 1]);
-			float m0 = __low2float(hr0) > 0.f ? 1.f : 0.f, m1 = __high2float(hr0) > 0.f ? 1.f : 0.f;
-			float m2 = __low2float(hr1) > 0.f ? 1.f : 0.f, m3 = __high2float(hr1) > 0.f ? 1.f : 0.f;
-			float v0 = fminf(fmaxf(c[nt][0] * m0, -scale_clip), scale_clip);
-			float v1 = fminf(fmaxf(c[nt][1] * m1, -scale_clip), scale_clip);
-			float v2 = fminf(fmaxf(c[nt][2] * m2, -scale_clip), scale_clip);
-			float v3 = fminf(fmaxf(c[nt][3] * m3, -scale_clip), scale_clip);
-			out[ks][2 * hh] = h2u(__floats2half2_rn(v0, v1));
-			out[ks][2 * hh + 1] = h2u(__floats2half2_rn(v2, v3));
+		for (int c = 0; c < 4; ++c) {
+			uint32_t w4[4];
+#pragma unroll
+			for (int e = 0; e < 4; ++e) {
+				const int col = 8 * c + 2 * e, j = 32 * h + col;
+				float lo = __uint_as_float(r[col >> 4][col & 15]), hi = __uint_as_float(r[col >> 4][(col & 15) + 1]);
+				if (relu) {
+					w4[e] = pack_relu_h2(lo, hi);
+					bits |= (uint64_t)((w4[e] & 0x7fffu) != 0u) << j;
+					bits |= (uint64_t)((w4[e] & 0x7fff0000u) != 0u) << (j + 1);
+				} else {
+					lo = ((mask >> j) & 1u) ? fminf(fmaxf(lo, -clip), clip) : 0.f;
+					hi = ((mask >> (j + 1)) & 1u) ? fminf(fmaxf(hi, -clip), clip) : 0.f;
+					w4[e] = pack_h2(lo, hi);
+				}
+			}
+			const uint4 v = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+			*reinterpret_cast<uint4 *>(hrow + (4 * h + c) * 128) = v;
+			if (g) g[4 * h + c] = v;
 		}
 	}
+	return bits;
 }
 
-// store A fragments of a 16 x 64 tile to rows r0/r1 of a [n][64] half array
-__device__ __forceinline__ void store_a64(const uint32_t (*a)[4], __half *base, int r0, int r1, int n) {
-	const int t = threadIdx.x & 3;
-#pragma unroll
-	for (int ks = 0; ks < 4; ++ks) {
-		if (r0 < n) {
-			*reinterpret_cast<uint32_t *>(base + (size_t)r0 * GN_H + ks * 16 + 2 * t) = a[ks][0];
-			*reinterpret_cast<uint32_t *>(base + (size_t)r0 * GN_H + ks * 16 + 8 + 2 * t) = a[ks][2];
-		}
-		if (r1 < n) {
-			*reinterpret_cast<uint32_t *>(base + (size_t)r1 * GN_H + ks * 16 + 2 * t) = a[ks][1];
-			*reinterpret_cast<uint32_t *>(base + (size_t)r1 * GN_H + ks * 16 + 8 + 2 * t) = a[ks][3];
-		}
-	}
-}
-
-__global__ void __launch_bounds__(GT, 1) k_guide_fwdbwd(const __half *__restrict__ img, const float *__restrict__ bias,
-	const float *__restrict__ samples, int n, float wscale, const float *__restrict__ wscale_dev, float wclip, float lscale,
-	GuideTrainBufs B, float *__restrict__ loss_sum) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_guide_fwdbwd_tc(const __half *__restrict__ tc_img,
+	const float *__restrict__ samples, int n, float wscale, const float *__restrict__ wscale_dev, float wclip,
+	float lscale, GuideTrainBufs B, float *__restrict__ loss_sum, unsigned *__restrict__ overflow,
+	unsigned *__restrict__ err) {
 	if (wscale_dev) wscale = *wscale_dev > 0.f ? (float)n / *wscale_dev : 0.f;  // device sum of the weights
 	extern __shared__ __align__(16) unsigned char smem[];
-	__half *s_img = reinterpret_cast<__half *>(smem);
-	float *s_bias = reinterpret_cast<float *>(smem + IMG_ALL * sizeof(__half));
-	float *s_out = s_bias + IMG_BIAS;  // per warp 16 x 48 FP32 outputs
-	__half *s_d5 = reinterpret_cast<__half *>(s_out + (GT / 32) * 16 * GN_OUT);  // per warp 16 x S_OUT
-	load_image(img, bias, IMG_ALL, s_img, s_bias);
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	float *wo = s_out + warp * 16 * GN_OUT;
-	__half *wd = s_d5 + warp * 16 * S_OUT;
+	uint64_t *bar = reinterpret_cast<uint64_t *>(smem + TT_OFF_BAR);  // [0] weights, [1 + wg] MMAs of warpgroup wg
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1 + TC_WG);
+	volatile uint32_t *fail = tmem_slot + 1;  // per warpgroup
+
+	const int tid = threadIdx.x, wg = tid >> 7, lt = tid & 127, warp = tid >> 5;
+	const int tiles = (n + 127) / 128;
+	if (blockIdx.x * TC_WG >= tiles) return;
+	if (tid == 0) {
+		for (int b = 0; b < 1 + TC_WG; ++b) mbar_init(&bar[b], 1);
+		for (int w = 0; w < TC_WG; ++w) fail[w] = 0;
+		mbar_init_fence();
+	}
+	if (warp == 0) {
+		tmem_alloc(tmem_slot, TC_COLS);
+		tmem_relinquish();
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tbase = *tmem_slot;
+	if (tid == 0) {
+		mbar_arrive_expect_tx(&bar[0], (uint32_t)((TC_HALVES + TCB_HALVES) * 2));
+		bulk_g2s(smem, tc_img, (uint32_t)((TC_HALVES + TCB_HALVES) * 2), &bar[0]);
+	}
+	if (lt == 0 && !mbar_wait(&bar[0], 0, TC_POLL_LIMIT)) fail[wg] = 1;
+
+	unsigned char *A = smem + TT_OFF_A + (size_t)wg * TC_A_BYTES;
+	const uint32_t a_addr = smem_addr(A), w_addr = smem_addr(smem), wt_addr = w_addr + TC_HALVES * 2;
+	const uint32_t tcol = tbase + (uint32_t)wg * 128u;
+	const uint32_t tlane = (uint32_t)((warp & 3) * 32) << 16;
+	const uint32_t bar_id = 1 + wg;
+	const uint32_t idesc_h = umma_idesc_f16(128, GN_H), idesc_o = umma_idesc_f16(128, GN_OUT);
+	uint32_t phase = 0;
+	uint64_t *mbar = &bar[1 + wg];
+	unsigned char *e0row = A + (lt >> 3) * TC_SBO_E0 + (lt & 7) * 16;
+	unsigned char *e1row = A + (lt >> 3) * TC_SBO_E1 + (lt & 7) * 16;
+	unsigned char *hrow = A + (lt >> 3) * TC_SBOH + (lt & 7) * 16;
+	// stages 0..5: the forward (as k_guide_infer); 6..9: the backward through layers 5, 4, 3, 2
+	auto sync_issue = [&](int stage) -> bool {
+		fence_proxy_async_smem();
+		tc_fence_before();
+		named_bar(bar_id, 128);
+		if (fail[wg]) return false;
+		if (lt == 0) {
+			tc_fence_after();
+			if (stage == 0) {
+				tc_mmas(tcol, a_addr, TC_SBO_E0, w_addr + TC_W1 * 2, TC_SBO1, 8, idesc_h, false);
+			} else if (stage == 1) {
+				tc_mmas(tcol, a_addr, TC_SBO_E1, w_addr + TC_W1 * 2 + 256u * 8, TC_SBO1, 7, idesc_h, true);
+			} else if (stage <= 5) {
+				tc_mmas(tcol + (stage == 5 ? 64u : 0u), a_addr, TC_SBOH,
+					w_addr + (stage == 2 ? TC_W2 : stage == 3 ? TC_W3 : stage == 4 ? TC_W4 : TC_W5) * 2, TC_SBOH, TC_KH / 16,
+					stage == 5 ? idesc_o : idesc_h, false);
+			} else {
+				const int K = stage == 6 ? TCB_K5 : GN_H;
+				const int off = stage == 6 ? TCB_W5 : stage == 7 ? TCB_W4 : stage == 8 ? TCB_W3 : TCB_W2;
+				tc_mmas(tcol, a_addr, TC_SBOH, wt_addr + off * 2, (uint32_t)K * 16u, K / 16, idesc_h, false);
+			}
+			umma_commit(mbar);
+		}
+		return true;
+	};
+	auto wait_mma = [&]() {
+		if (lt == 0) {
+			if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+			tc_fence_before();
+		}
+		phase ^= 1u;
+		named_bar(bar_id, 128);
+		tc_fence_after();
+	};
+	named_bar(bar_id, 128);
 	const float clip = 60000.f;
 	float lacc = 0.f;
-	const int tiles = (n + 15) / 16;
-	for (int tile = blockIdx.x * (GT / 32) + warp; tile < tiles; tile += gridDim.x * (GT / 32)) {
-		int r0 = tile * 16 + g, r1 = r0 + 8;
-		float x0[GN_IN], x1[GN_IN];
-		for (int k = 0; k < GN_IN; ++k) {
-			x0[k] = r0 < n ? samples[(size_t)r0 * 16 + k] : 0.f;
-			x1[k] = r1 < n ? samples[(size_t)r1 * 16 + k] : 0.f;
-		}
-		float c5[6][4];
-		uint32_t hk[4][4][4];
-		tile_forward(s_img, s_bias, x0, x1, c5, hk, B.h0 + (size_t)(r0 < n ? r0 : B.dump_row) * GN_ENC,
-			B.h0 + (size_t)(r1 < n ? r1 : B.dump_row) * GN_ENC);
-		// outputs to shared memory, one row per lane for the loss
+	for (int tile = blockIdx.x * TC_WG + wg; tile < tiles; tile += gridDim.x * TC_WG) {
+		const int row = tile * 128 + lt;
+		const bool valid = row < n;
+		float x[GN_IN];
 #pragma unroll
-		for (int nt = 0; nt < 6; ++nt) {
-			wo[g * GN_OUT + nt * 8 + 2 * t] = c5[nt][0];
-			wo[g * GN_OUT + nt * 8 + 2 * t + 1] = c5[nt][1];
-			wo[(g + 8) * GN_OUT + nt * 8 + 2 * t] = c5[nt][2];
-			wo[(g + 8) * GN_OUT + nt * 8 + 2 * t + 1] = c5[nt][3];
+		for (int k = 0; k < GN_IN; ++k) x[k] = valid ? samples[(size_t)row * 16 + k] : 0.0f;
+		uint4 *h0g = valid ? reinterpret_cast<uint4 *>(B.h0 + (size_t)row * GN_ENC) : nullptr;
+		// layer 1: the encoding in two K halves, each also stored for the weight gradients
+#pragma unroll
+		for (int c = 0; c < 16; ++c) {
+			const uint4 v = enc_chunk(x, c);
+			*reinterpret_cast<uint4 *>(e0row + c * 128) = v;
+			if (h0g) h0g[c] = v;
 		}
-		__syncwarp();
-		if (lane < 16) {
-			int r = tile * 16 + lane;
-			float gr[GN_OUT];
+		if (!sync_issue(0)) break;
+		wait_mma();
+#pragma unroll
+		for (int c = 16; c < 30; ++c) {
+			const uint4 v = enc_chunk(x, c);
+			*reinterpret_cast<uint4 *>(e1row + (c - 16) * 128) = v;
+			if (h0g) h0g[c] = c == 28 ? make_uint4(v.x & 0xffffu, 0u, 0u, 0u) : v;  // the master layout's 0 in column 225
+		}
+		if (h0g) h0g[30] = h0g[31] = make_uint4(0u, 0u, 0u, 0u);
+		if (!sync_issue(1)) break;
+		wait_mma();
+		// layers 2..5: the hidden activations h1..h4 (stored, their masks kept) feed the next layer
+		uint64_t mk[4];
+		bool ok = true;
+#pragma unroll 1
+		for (int layer = 2; layer <= 5 && ok; ++layer) {
+			uint4 *hg = valid ? reinterpret_cast<uint4 *>(B.h[layer - 2] + (size_t)row * GN_H) : nullptr;
+			mk[layer - 2] = tt_epilogue(tcol + tlane, hrow, hg, true, 0ull, clip);
+			if (layer == 2) {
+				*reinterpret_cast<uint4 *>(hrow + 8 * 128) = make_uint4(pack_h2(1.f, 0.f), 0u, 0u, 0u);
+				*reinterpret_cast<uint4 *>(hrow + 9 * 128) = make_uint4(0u, 0u, 0u, 0u);
+			}
+			ok = sync_issue(layer);
+			if (ok) wait_mma();
+		}
+		if (!ok) break;
+		// the output gradient of the row (K = 48 of the next product: 40 used, then zeros)
+		{
+			uint32_t r[3][16];
+#pragma unroll
+			for (int g = 0; g < 3; ++g) tmem_ld16(tcol + 64u + tlane + 16u * g, r[g]);
+			tmem_ld_wait();
+			float o[5 * GN_LOBES], gr[GN_OUT];
+#pragma unroll
+			for (int col = 0; col < 5 * GN_LOBES; ++col) o[col] = __uint_as_float(r[col >> 4][col & 15]);
+#pragma unroll
 			for (int j = 0; j < GN_OUT; ++j) gr[j] = 0.f;
-			if (r < n) {
-				const float *s = samples + (size_t)r * 16;
-				float wt = fminf(s[12] * wscale, wclip);
-				lacc += sample_out_grad(wo + lane * GN_OUT, f3{ s[9], s[10], s[11] }, wt, gr);
+			if (valid) {
+				const float *s = samples + (size_t)row * 16;
+				const float wt = fminf(s[12] * wscale, wclip);
+				lacc += sample_out_grad(o, f3{ s[9], s[10], s[11] }, wt, gr);
 			}
-			for (int j = 0; j < GN_OUT; ++j) {
-				float v = fminf(fmaxf(gr[j] * lscale, -clip), clip);
-				wd[lane * S_OUT + j] = __float2half_rn(v);
-				if (r < n) B.d5[(size_t)r * GN_OUT + j] = wd[lane * S_OUT + j];
-			}
-		}
-		__syncwarp();
-		// backward: delta5 (16 x 48) -> delta4 .. delta1
-		uint32_t da5[3][4];
+			uint4 *dg = valid ? reinterpret_cast<uint4 *>(B.d5 + (size_t)row * GN_OUT) : nullptr;
 #pragma unroll
-		for (int ks = 0; ks < 3; ++ks) {
-			da5[ks][0] = *reinterpret_cast<const uint32_t *>(wd + g * S_OUT + ks * 16 + 2 * t);
-			da5[ks][1] = *reinterpret_cast<const uint32_t *>(wd + (g + 8) * S_OUT + ks * 16 + 2 * t);
-			da5[ks][2] = *reinterpret_cast<const uint32_t *>(wd + g * S_OUT + ks * 16 + 8 + 2 * t);
-			da5[ks][3] = *reinterpret_cast<const uint32_t *>(wd + (g + 8) * S_OUT + ks * 16 + 8 + 2 * t);
+			for (int c = 0; c < GN_OUT / 8; ++c) {
+				uint32_t w4[4];
+#pragma unroll
+				for (int e = 0; e < 4; ++e)
+					w4[e] = pack_h2(fminf(fmaxf(gr[8 * c + 2 * e] * lscale, -clip), clip),
+						fminf(fmaxf(gr[8 * c + 2 * e + 1] * lscale, -clip), clip));
+				const uint4 v = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+				*reinterpret_cast<uint4 *>(hrow + c * 128) = v;
+				if (dg) dg[c] = v;
+			}
 		}
-		uint32_t d4[4][4], d3[4][4], d2[4][4], d1[4][4];
-		back_layer<3>(da5, s_img + IMG_W5T, S_OUT, hk[3], d4, clip);
-		back_layer<4>(d4, s_img + IMG_W4T, S_H, hk[2], d3, clip);
-		back_layer<4>(d3, s_img + IMG_W3T, S_H, hk[1], d2, clip);
-		back_layer<4>(d2, s_img + IMG_W2T, S_H, hk[0], d1, clip);
-		store_a64(d4, B.d[3], r0, r1, n);
-		store_a64(d3, B.d[2], r0, r1, n);
-		store_a64(d2, B.d[1], r0, r1, n);
-		store_a64(d1, B.d[0], r0, r1, n);
-		for (int L = 0; L < 4; ++L) store_a64(hk[L], B.h[L], r0, r1, n);
-		__syncwarp();
+		// backward: gradients at h4, h3, h2, h1
+#pragma unroll 1
+		for (int stage = 6; stage <= 9 && ok; ++stage) {
+			ok = sync_issue(stage);
+			if (!ok) break;
+			wait_mma();
+			const int L = 9 - stage;  // the gradient at h(L + 1): B.d[L], masked by mk[L]
+			uint4 *dg = valid ? reinterpret_cast<uint4 *>(B.d[L] + (size_t)row * GN_H) : nullptr;
+			tt_epilogue(tcol + tlane, hrow, dg, false, mk[L], clip);
+		}
+		if (!ok) break;
+		tc_fence_before();
+	}
+	named_bar(bar_id, 128);
+	if (lt == 0 && fail[wg]) {
+		atomicOr(err, (unsigned)ERR_TENSOR_TIMEOUT);
+		atomicOr(overflow, 1u);
+		mbar_wait(&bar[0], 0, TC_POLL_LIMIT);
+		mbar_wait(mbar, phase ^ 1u, TC_POLL_LIMIT);
 	}
 	for (int o = 16; o > 0; o >>= 1) lacc += __shfl_down_sync(0xffffffffu, lacc, o);
-	if (lane == 0) atomicAdd(loss_sum, lacc);
+	if ((tid & 31) == 0 && lacc != 0.f) atomicAdd(loss_sum, lacc);
+	tc_fence_before();
+	__syncthreads();
+	if (warp == 0) {
+		tc_fence_after();
+		tmem_dealloc(tbase, TC_COLS);
+	}
 }
 
 // dW[o][i] += sum over a chunk of samples of delta[s][o] * h[s][i] on the tensor
@@ -729,11 +767,6 @@ are_status bad(const std::string &m) {
 }  // namespace
 
 size_t guide_infer_smem() { return TC_SMEM; }
-size_t guide_train_smem() {
-	return IMG_ALL * sizeof(__half) + IMG_BIAS * sizeof(float) + (GT / 32) * 16 * GN_OUT * sizeof(float) +
-		(GT / 32) * 16 * S_OUT * sizeof(__half);
-}
-
 GuideNet::~GuideNet() {
 	if (stream) cudaStreamSynchronize(stream);
 	for (void *p : allocs) cudaFree(p);
@@ -755,13 +788,11 @@ are_status GuideNet::init(uint64_t seed) {
 	if (are_status st = alloc((void **)&adam_m, GN_PARAMS * sizeof(float))) return st;
 	if (are_status st = alloc((void **)&adam_v, GN_PARAMS * sizeof(float))) return st;
 	if (are_status st = alloc((void **)&grad, (GN_PARAMS + 64) * sizeof(float))) return st;
-	if (are_status st = alloc((void **)&img, IMG_ALL * sizeof(__half))) return st;
-	if (are_status st = alloc((void **)&bias, IMG_BIAS * sizeof(float))) return st;
-	if (are_status st = alloc((void **)&tc_img, TC_HALVES * sizeof(__half))) return st;
+	if (are_status st = alloc((void **)&tc_img, (TC_HALVES + TCB_HALVES) * sizeof(__half))) return st;
 	if (are_status st = alloc((void **)&err_word, 16)) return st;
 	if (cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_infer_smem()) != cudaSuccess ||
-		cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)guide_train_smem()) != cudaSuccess ||
-		cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WG_SMEM) != cudaSuccess)
+		cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WG_SMEM) != cudaSuccess ||
+		cudaFuncSetAttribute(k_guide_fwdbwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_SMEM) != cudaSuccess)
 		return cuda_status(cudaGetLastError(), "cudaFuncSetAttribute(guide)");
 	// seeded He-uniform initialisation on the host (SplitMix64 stream)
 	std::vector<float> h(GN_PARAMS, 0.0f);
@@ -795,9 +826,8 @@ are_status GuideNet::set_params(const float *host) {
 }
 
 are_status GuideNet::pack() {
-	k_guide_pack<<<128, 256, 0, stream>>>(params, img, bias);
 	k_guide_pack_tc<<<68, 256, 0, stream>>>(params, tc_img);
-	return cuda_status(cudaGetLastError(), "k_guide_pack");
+	return cuda_status(cudaGetLastError(), "k_guide_pack_tc");
 }
 
 are_status GuideNet::ensure_train(int n) {
@@ -807,11 +837,9 @@ are_status GuideNet::ensure_train(int n) {
 	train_mem = nullptr;
 	train_cap = 0;
 	size_t per = (size_t)(GN_ENC + 8 * GN_H + GN_OUT) * sizeof(__half);
-	if (are_status st = cuda_status(cudaMalloc(&train_mem, per * cap + 16 * GN_ENC * sizeof(__half) + 1024), "cudaMalloc(guide training)"))
-		return st;
+	if (are_status st = cuda_status(cudaMalloc(&train_mem, per * cap + 1024), "cudaMalloc(guide training)")) return st;
 	__half *p = (__half *)train_mem;
-	bufs.h0 = p, p += (size_t)(cap + 16) * GN_ENC;
-	bufs.dump_row = cap;
+	bufs.h0 = p, p += (size_t)cap * GN_ENC;
 	for (int L = 0; L < 4; ++L) bufs.h[L] = p, p += (size_t)cap * GN_H;
 	for (int L = 0; L < 4; ++L) bufs.d[L] = p, p += (size_t)cap * GN_H;
 	bufs.d5 = p;
@@ -847,8 +875,6 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 		cudaMemsetAsync(bufs.d5 + (size_t)n * GN_OUT, 0, (size_t)(nz - n) * GN_OUT * 2, s);
 		cudaMemsetAsync(bufs.h0 + (size_t)n * GN_ENC, 0, (size_t)(nz - n) * GN_ENC * 2, s);
 	}
-	int tiles = np / 16;
-	int grid = std::max(1, std::min(n_sms, (tiles + 7) / 8));
 	// wmean < 0: the batch's mean weight is computed on the device
 	const float *wdev = nullptr;
 	float wscale = wmean > 0.f ? 1.0f / wmean : 0.f;
@@ -856,8 +882,11 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 		k_weight_sum<<<std::max(1, std::min(n_sms, (n + 255) / 256)), 256, 0, s>>>(d_samples, n, grad + GN_PARAMS + 2);
 		wdev = grad + GN_PARAMS + 2;
 	}
-	k_guide_fwdbwd<<<grid, GT, guide_train_smem(), s>>>(img, bias, d_samples, n, wscale, wdev, weight_clip, loss_scale,
-		bufs, grad + GN_PARAMS);
+	// one block (four warpgroups, one 128-row tile each at a time) per SM at most
+	const int tiles = (n + 127) / 128;
+	const int grid = std::max(1, std::min(n_sms, (tiles + TC_WG - 1) / TC_WG));
+	k_guide_fwdbwd_tc<<<grid, TC_THREADS, TT_SMEM, s>>>(tc_img, d_samples, n, wscale, wdev, weight_clip, loss_scale, bufs,
+		grad + GN_PARAMS, (unsigned *)(grad + GN_PARAMS + 1), err_word);
 	const int blocks = WG_BLOCKS_PER_SM * n_sms;
 	const int chunk = std::max(WG_SUB, ((np + blocks - 1) / blocks + WG_SUB - 1) / WG_SUB * WG_SUB);
 	k_guide_wgrad<<<(np + chunk - 1) / chunk, GT, WG_SMEM, s>>>(bufs, np, chunk, grad, (unsigned *)(grad + GN_PARAMS + 1));
@@ -870,7 +899,6 @@ are_status GuideNet::train_step(const float *d_samples, int n, float wmean, floa
 	float c1 = 1.f - std::pow(0.9f, (float)steps), c2 = 1.f - std::pow(0.99f, (float)steps);
 	k_guide_adam<<<64, 256, 0, s>>>(params, adam_m, adam_v, grad, 1.0f / (loss_scale * (float)n), lr, 0.9f, 0.99f, 1e-8f,
 		c1, c2, (const unsigned *)(grad + GN_PARAMS + 1));
-	k_guide_pack<<<128, 256, 0, s>>>(params, img, bias);
 	k_guide_pack_tc<<<68, 256, 0, s>>>(params, tc_img);
 	return cuda_status(cudaGetLastError(), "guide Adam");
 }

@@ -4,9 +4,11 @@
 //
 // The network and its loss are specified in oracle/orc_guide.c (FP64); the
 // device computes the same in FP16 on the tensor cores with FP32
-// accumulation (mma.sync.m16n8k16, activations kept in registers between
-// layers as in the fully fused MLPs of Mueller et al., "Real-time Neural
-// Radiance Caching", 2021), FP32 master weights and Adam.
+// accumulation: the forward and backward passes fused per 128-row tile on the
+// 5th-generation tensor cores (tcgen05, guide.cu), in the manner of the fully
+// fused MLPs of Mueller et al., "Real-time Neural Radiance Caching", 2021; the
+// weight gradients reduce over the batch with mma.sync.m16n8k16; FP32 master
+// weights and Adam.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -26,23 +28,7 @@ constexpr int OFF_W4 = OFF_B3 + GN_H, OFF_B4 = OFF_W4 + GN_H * GN_H;
 constexpr int OFF_W5 = OFF_B4 + GN_H, OFF_B5 = OFF_W5 + GN_OUT * GN_H;
 constexpr int GN_PARAMS = OFF_B5 + GN_OUT;
 
-// FP16 weight image, copied whole into shared memory.  Row strides are padded
-// by 8 halves so the B-fragment loads of a warp hit 32 distinct banks.
-constexpr int S_ENC = GN_ENC + 8, S_H = GN_H + 8, S_OUT = GN_OUT + 8;
-constexpr int IMG_W1 = 0;                          // [64][S_ENC]   forward
-constexpr int IMG_W2 = IMG_W1 + GN_H * S_ENC;      // [64][S_H]
-constexpr int IMG_W3 = IMG_W2 + GN_H * S_H;
-constexpr int IMG_W4 = IMG_W3 + GN_H * S_H;
-constexpr int IMG_W5 = IMG_W4 + GN_H * S_H;        // [48][S_H]
-constexpr int IMG_FWD = IMG_W5 + GN_OUT * S_H;     // halves of the forward image
-constexpr int IMG_W2T = IMG_FWD;                   // [64 in][S_H] transposed, backward
-constexpr int IMG_W3T = IMG_W2T + GN_H * S_H;
-constexpr int IMG_W4T = IMG_W3T + GN_H * S_H;
-constexpr int IMG_W5T = IMG_W4T + GN_H * S_H;      // [64 in][S_OUT]
-constexpr int IMG_ALL = IMG_W5T + GN_H * S_OUT;    // halves of forward + backward image
-constexpr int IMG_BIAS = 4 * GN_H + GN_OUT;        // FP32 biases after the halves
-
-// Weight image of the tcgen05 inference kernel (halves): each layer's
+// Weight image of the tcgen05 kernels (halves): each layer's
 // [out][in] matrix in the canonical no-swizzle K-major layout of the tensor
 // core (core matrices of 8 rows x 8 halves, 64 halves each; the core matrices
 // of one 8-row group adjacent in K).  The biases ride in the GEMMs: layer 1
@@ -63,6 +49,16 @@ constexpr int TC_HALVES = TC_W5 + GN_OUT * TC_KH;
 __host__ __device__ constexpr int tc_index(int row, int k, int K) {
 	return (row >> 3) * (K * 8) + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
 }
+// The backward image, right after the forward one in the same buffer: the
+// transposed weights W^T ([in][out], K = the layer's outputs) of layers 5..2
+// in the same layout, whose product with a row's gradient at a layer's output
+// is the gradient at its input.  Layer 5 keeps K = 48 (outputs 40..47 zero).
+constexpr int TCB_K5 = GN_OUT;
+constexpr int TCB_W5 = 0;                       // [64][48]
+constexpr int TCB_W4 = TCB_W5 + GN_H * TCB_K5;  // [64][64]
+constexpr int TCB_W3 = TCB_W4 + GN_H * GN_H;
+constexpr int TCB_W2 = TCB_W3 + GN_H * GN_H;
+constexpr int TCB_HALVES = TCB_W2 + GN_H * GN_H;
 
 // features of a shading point: position scaled to the scene box, normal, outgoing direction
 struct GuideBox {
@@ -78,38 +74,8 @@ __device__ __forceinline__ void guide_features(const GuideBox &B, f3 p, f3 n, f3
 }
 
 // The input encoding is 128 pairs of FP16 values: pair 12 i + k (i < 9,
-// k < 12) is (sin, cos)(pi 2^k x_i), pairs 108..112 the raw features two by
-// two (the last one padded with 0), the rest zero.
-//
-// Lane t of a quad holds pair indices b + t with b a
-// multiple of 4 (a constant once the caller's loop is unrolled).  For b < 108
-// that is feature i = b / 12 at frequency k = b % 12 + t, and b % 12 runs
-// through 0, 4, 8 for each feature in turn.  Frequencies t and t + 8 take a
-// sincospif each; t + 4 comes from t by four angle doublings (sin 2a =
-// 2 sin a cos a, cos 2a = (cos a - sin a)(cos a + sin a)), which grow the FP32
-// rounding error 16-fold, to about 2e-5: below the FP16 rounding of the result.
-__device__ __forceinline__ __half2 enc_quad(const float *x, int b, int t, float &s, float &c) {
-	if (b < 108) {
-		const int i = b / 12;
-		if (b % 12 != 4) {
-			sincospif(ldexpf(x[i], t + b % 12), &s, &c);
-		} else {
-#pragma unroll
-			for (int d = 0; d < 4; ++d) {  // 2^4: angle doublings from k to k + 4
-				float s2 = 2.f * s * c, c2 = (c - s) * (c + s);
-				s = s2, c = c2;
-			}
-		}
-		return __floats2half2_rn(s, c);
-	}
-	if (b == 108) {  // raw features (x[2t], x[2t+1])
-		float u = t == 0 ? x[0] : t == 1 ? x[2] : t == 2 ? x[4] : x[6];
-		float v = t == 0 ? x[1] : t == 1 ? x[3] : t == 2 ? x[5] : x[7];
-		return __floats2half2_rn(u, v);
-	}
-	if (b == 112) return __floats2half2_rn(t == 0 ? x[8] : 0.0f, 0.0f);
-	return __floats2half2_rn(0.0f, 0.0f);
-}
+// k < 12) is (sin, cos)(pi 2^k x_i), pairs 108..111 the raw features x_0..x_7
+// two by two, pair 112 (x_8, 0), the rest zero (guide.cu: enc_chunk).
 
 __device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t *>(&h); }
 __device__ __forceinline__ __half2 u2h(uint32_t u) { return *reinterpret_cast<__half2 *>(&u); }
@@ -120,42 +86,6 @@ __device__ __forceinline__ void mma16816(float *c, const uint32_t *a, uint32_t b
 		"{%0,%1,%2,%3};\n"
 		: "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
 		: "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// One dense layer on a 16-row tile: C[nt] (16 x 8 per n-tile) += A (16 x K) W^T
-// with W an [out][in] half matrix of row stride `stride` in shared memory.
-// A is given as K/16 groups of 4 fragment registers.
-template <int KSTEPS, int NTILES>
-__device__ __forceinline__ void tile_layer(const uint32_t (*a)[4], const __half *W, int stride, float (*c)[4]) {
-	const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-#pragma unroll
-	for (int nt = 0; nt < NTILES; ++nt) {
-		c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-		const __half *row = W + (nt * 8 + g) * stride + 2 * t;
-#pragma unroll
-		for (int ks = 0; ks < KSTEPS; ++ks) {
-			uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + ks * 16);
-			uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + ks * 16 + 8);
-			mma16816(c[nt], a[ks], b0, b1);
-		}
-	}
-}
-
-// C fragments of a 16 x 64 layer (+bias, ReLU) -> A fragments of the next layer.
-__device__ __forceinline__ void relu_to_a(float (*c)[4], const float *bias, uint32_t (*a)[4]) {
-	const int t = threadIdx.x & 3;
-#pragma unroll
-	for (int ks = 0; ks < 4; ++ks) {
-#pragma unroll
-		for (int h = 0; h < 2; ++h) {
-			int nt = 2 * ks + h;
-			float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
-			float v0 = fmaxf(c[nt][0] + b0, 0.f), v1 = fmaxf(c[nt][1] + b1, 0.f);
-			float v2 = fmaxf(c[nt][2] + b0, 0.f), v3 = fmaxf(c[nt][3] + b1, 0.f);
-			a[ks][2 * h] = h2u(__floats2half2_rn(v0, v1));
-			a[ks][2 * h + 1] = h2u(__floats2half2_rn(v2, v3));
-		}
-	}
 }
 
 // ---- the vMF mixture -------------------------------------------------------

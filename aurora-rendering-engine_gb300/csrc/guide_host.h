@@ -1,6 +1,6 @@
 // guide_host.h — host-side owner of a path-guiding network (the opaque
 // are_guide of the C ABI): FP32 master parameters, Adam moments, the FP16
-// weight image the kernels load, and the training buffers.
+// weight images the kernels load, and the training buffers.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -15,11 +15,10 @@ namespace are_core {
 
 // per-sample tensors of one training batch, FP16 [samples][features]
 struct GuideTrainBufs {
-	__half *h0;     // encoded inputs [cap + 16][256] (row cap+ is a write-only dump row)
+	__half *h0;     // encoded inputs [cap][256]
 	__half *h[4];   // hidden outputs h1..h4 [cap][64]
 	__half *d[4];   // gradients at h1..h4 pre-activations [cap][64]
 	__half *d5;     // output gradients [cap][48]
-	int dump_row;
 };
 
 struct GuideNet {
@@ -28,9 +27,7 @@ struct GuideNet {
 	bool own_stream = false;
 	float *params = nullptr, *adam_m = nullptr, *adam_v = nullptr;
 	float *grad = nullptr;  // GN_PARAMS gradients, then loss sum, then an overflow flag
-	__half *img = nullptr;     // FP16 weights for the training kernels (row-major, padded strides)
-	__half *tc_img = nullptr;  // FP16 weights for the tensor-core inference kernel (core-matrix layout)
-	float *bias = nullptr;
+	__half *tc_img = nullptr;  // FP16 weights of the tensor-core kernels (core-matrix layout): forward, then backward
 	unsigned *err_word = nullptr;  // device error bits of inference outside a render
 	void *train_mem = nullptr;
 	int train_cap = 0;
@@ -58,7 +55,6 @@ struct GuideNet {
 };
 
 size_t guide_infer_smem();
-size_t guide_train_smem();
 
 are_status render_guided(struct ::are_scene *sc, GuideNet *net, const are_camera *cam, const are_render_params *prm,
 	const are_guide_params *gp, float *rgb, float *var, are_render_stats *stats);
