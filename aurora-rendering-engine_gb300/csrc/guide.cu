@@ -415,7 +415,7 @@ __device__ __forceinline__ uint64_t tt_epilogue(uint32_t taddr, unsigned char *h
 __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_fwdbwd_tc(const __half *__restrict__ tc_img,
 	const float *__restrict__ samples, int n, float wscale, const float *__restrict__ wscale_dev, float wclip,
 	float lscale, GuideTrainBufs B, float *__restrict__ loss_sum, unsigned *__restrict__ overflow,
-	unsigned *__restrict__ err) {
+	unsigned *__restrict__ err, uint32_t first_limit) {
 	if (wscale_dev) wscale = *wscale_dev > 0.f ? (float)n / *wscale_dev : 0.f;  // device sum of the weights
 	extern __shared__ __align__(16) unsigned char smem[];
 	uint64_t *bar = reinterpret_cast<uint64_t *>(smem + TT_OFF_BAR);  // [0] weights, [1 + wg] MMAs of warpgroup wg
@@ -480,11 +480,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_guide_fwdbwd_tc(const __half 
 		}
 		return true;
 	};
+	// first_limit: polls allowed for each warpgroup's first MMA wait, as in k_guide_infer
+	uint32_t limit = min(first_limit, TC_POLL_LIMIT);
 	auto wait_mma = [&]() {
 		if (lt == 0) {
-			if (!mbar_wait(mbar, phase, TC_POLL_LIMIT)) fail[wg] = 1;
+			if (!mbar_wait(mbar, phase, limit)) fail[wg] = 1;
 			tc_fence_before();
 		}
+		limit = TC_POLL_LIMIT;
 		phase ^= 1u;
 		named_bar(bar_id, 128);
 		tc_fence_after();
@@ -861,7 +864,7 @@ are_status GuideNet::infer(const float *d_feat, int n, float *d_out, cudaStream_
 
 // samples: n x 16 device floats (features 9, direction 3, weight 1, 3 unused).
 // Accumulates the gradient (FP32, times the loss scale) in `grad` and the loss in grad[GN_PARAMS].
-are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaStream_t s) {
+are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaStream_t s, unsigned *d_err) {
 	if (are_status st = ensure_train(n)) return st;
 	int np = (n + 15) & ~15;
 	const int nz = (n + WG_SUB - 1) / WG_SUB * WG_SUB;
@@ -886,15 +889,15 @@ are_status GuideNet::gradient(const float *d_samples, int n, float wmean, cudaSt
 	const int tiles = (n + 127) / 128;
 	const int grid = std::max(1, std::min(n_sms, (tiles + TC_WG - 1) / TC_WG));
 	k_guide_fwdbwd_tc<<<grid, TC_THREADS, TT_SMEM, s>>>(tc_img, d_samples, n, wscale, wdev, weight_clip, loss_scale, bufs,
-		grad + GN_PARAMS, (unsigned *)(grad + GN_PARAMS + 1), err_word);
+		grad + GN_PARAMS, (unsigned *)(grad + GN_PARAMS + 1), d_err ? d_err : err_word, first_wait_limit);
 	const int blocks = WG_BLOCKS_PER_SM * n_sms;
 	const int chunk = std::max(WG_SUB, ((np + blocks - 1) / blocks + WG_SUB - 1) / WG_SUB * WG_SUB);
 	k_guide_wgrad<<<(np + chunk - 1) / chunk, GT, WG_SMEM, s>>>(bufs, np, chunk, grad, (unsigned *)(grad + GN_PARAMS + 1));
 	return cuda_status(cudaGetLastError(), "guide gradient kernels");
 }
 
-are_status GuideNet::train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s) {
-	if (are_status st = gradient(d_samples, n, wmean, s)) return st;
+are_status GuideNet::train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s, unsigned *d_err) {
+	if (are_status st = gradient(d_samples, n, wmean, s, d_err)) return st;
 	++steps;
 	float c1 = 1.f - std::pow(0.9f, (float)steps), c2 = 1.f - std::pow(0.99f, (float)steps);
 	k_guide_adam<<<64, 256, 0, s>>>(params, adam_m, adam_v, grad, 1.0f / (loss_scale * (float)n), lr, 0.9f, 0.99f, 1e-8f,
@@ -1056,10 +1059,17 @@ ARE_API are_status are_guide_gradient(are_guide *gh, const float *samples, int64
 		DevTmp t;
 		float wmean = 0.f;
 		if (are_status st = upload_samples(g, samples, n, t, wmean)) return st;
+		cudaMemsetAsync(g->err_word, 0, 4, g->stream);
 		if (are_status st = g->gradient((const float *)t.p, (int)n, wmean, g->stream)) return st;
 		std::vector<float> h(are_core::GN_PARAMS + 2);
 		cudaMemcpyAsync(h.data(), g->grad, h.size() * 4, cudaMemcpyDeviceToHost, g->stream);
+		unsigned herr = 0;
+		cudaMemcpyAsync(&herr, g->err_word, 4, cudaMemcpyDeviceToHost, g->stream);
 		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide gradient")) return st;
+		if (herr) {
+			are_core::set_error("guide gradient: device error word " + std::to_string(herr));
+			return ARE_ERR_KERNEL_TIMEOUT;
+		}
 		float s = 1.0f / (g->loss_scale * (float)n);
 		for (int i = 0; i < are_core::GN_PARAMS; ++i) grad[i] = h[i] * s;
 		if (loss) *loss = h[are_core::GN_PARAMS] / (float)n;
@@ -1106,10 +1116,18 @@ ARE_API are_status are_guide_train(are_guide *gh, const float *samples, int64_t 
 		DevTmp t;
 		float wmean = 0.f;
 		if (are_status st = upload_samples(g, samples, n, t, wmean)) return st;
+		cudaMemsetAsync(g->err_word, 0, 4, g->stream);
 		if (are_status st = g->train_step((const float *)t.p, (int)n, wmean, lr, g->stream)) return st;
 		float l = 0.f;
+		unsigned herr = 0;
 		cudaMemcpyAsync(&l, g->grad + are_core::GN_PARAMS, 4, cudaMemcpyDeviceToHost, g->stream);
+		cudaMemcpyAsync(&herr, g->err_word, 4, cudaMemcpyDeviceToHost, g->stream);
 		if (are_status st = are_core::cuda_status(cudaStreamSynchronize(g->stream), "guide train")) return st;
+		if (herr) {
+			// the step's gradients are incomplete: the kernel flagged them, and Adam left the weights as they were
+			are_core::set_error("guide train: device error word " + std::to_string(herr) + "; the step was skipped");
+			return ARE_ERR_KERNEL_TIMEOUT;
+		}
 		if (loss) *loss = l / (float)n;
 		return ARE_OK;
 	});

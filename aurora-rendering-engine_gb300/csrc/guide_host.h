@@ -36,7 +36,7 @@ struct GuideNet {
 	int64_t steps = 0;
 	float loss_scale = 8.0f;     // gradients are carried in FP16 times this factor
 	float weight_clip = 1e30f;   // cap on a sample's normalised weight
-	uint32_t first_wait_limit = 0xffffffffu;  // polls of each warpgroup's first MMA wait in inference (capped)
+	uint32_t first_wait_limit = 0xffffffffu;  // polls of each warpgroup's first MMA wait in inference and training (capped)
 	std::vector<float> loss_log; // losses of Adam steps taken inside renders
 
 	~GuideNet();
@@ -50,8 +50,9 @@ struct GuideNet {
 	are_status infer(const float *d_feat, int n, float *d_out, cudaStream_t s, const unsigned *n_dev = nullptr,
 		unsigned *d_err = nullptr, bool mixture_out = false);
 	// wmean < 0: normalise the weights by their batch mean computed on the device
-	are_status gradient(const float *d_samples, int n, float wmean, cudaStream_t s);
-	are_status train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s);
+	// d_err: device error word to OR failures into (default: err_word); a failed step is not applied
+	are_status gradient(const float *d_samples, int n, float wmean, cudaStream_t s, unsigned *d_err = nullptr);
+	are_status train_step(const float *d_samples, int n, float wmean, float lr, cudaStream_t s, unsigned *d_err = nullptr);
 };
 
 size_t guide_infer_smem();

@@ -458,7 +458,7 @@ are_status render_guided(are_scene *sc, GuideNet *net, const are_camera *cam, co
 			net->weight_clip = gp->weight_clip > 0.f ? gp->weight_clip : 1e30f;
 			cudaEventRecord(kev[4 * GUIDED_ITERS], s);
 			for (int k = 0; k < gp->train && !st; ++k) {
-				st = net->train_step(G.tbuf, (int)have, -1.0f, gp->lr, s);
+				st = net->train_step(G.tbuf, (int)have, -1.0f, gp->lr, s, W.cnt + 4);
 				++train_steps;
 				launches[ARE_KERNEL_OTHER] += 7;
 			}

@@ -565,7 +565,7 @@ are_status render_guided_mega(are_scene *sc, GuideNet *net, const are_camera *ca
 			cudaEventRecord(ev[6], s);
 			for (unsigned b = 0; b < nb && !st; ++b)
 				for (int k = 0; k < gp->train && !st && (gp->max_steps <= 0 || train_steps < gp->max_steps); ++k) {
-					st = net->train_step(G.tbuf + (size_t)b * batch * 16, (int)rows, -1.0f, gp->lr, s);
+					st = net->train_step(G.tbuf + (size_t)b * batch * 16, (int)rows, -1.0f, gp->lr, s, W.cnt + 4);
 					++train_steps;
 					launches[ARE_KERNEL_OTHER] += 7;
 				}

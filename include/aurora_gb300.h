@@ -314,14 +314,15 @@ ARE_API int32_t are_guide_loss_history(are_guide *guide, float *out, int32_t max
 /* one Adam step (beta1 0.9, beta2 0.99) on a batch; loss before the step */
 ARE_API are_status are_guide_train(are_guide *guide, const float *samples, int64_t n, float lr, float *loss);
 
-/* Test hook for the bounded device-side waits of the tensor-core inference:
- * each warpgroup's first wait for its tensor-core MMAs gives up after `polls`
- * polls (-1 restores the default bound of 2^22).  A wait that gives up sets
- * the device error bit 16, lets the work already in flight land, frees the
- * block's tensor memory and returns, and the call reports
- * ARE_ERR_KERNEL_TIMEOUT (inside a render, ARE_ERR_INTERNAL); with polls = 0
- * every inference call of this guide takes that path.  No counterpart in the
- * reference. */
+/* Test hook for the bounded device-side waits of the tensor-core inference
+ * and training kernels: each warpgroup's first wait for its tensor-core MMAs
+ * gives up after `polls` polls (-1 restores the default bound of 2^22).  A
+ * wait that gives up sets the device error bit 16, lets the work already in
+ * flight land, frees the block's tensor memory and returns, and the call
+ * reports ARE_ERR_KERNEL_TIMEOUT (inside a render, ARE_ERR_INTERNAL); a
+ * training step that gave up is not applied (the weights stay as they
+ * were).  With polls = 0 every inference and training call of this guide
+ * takes that path.  No counterpart in the reference. */
 ARE_API are_status are_guide_set_wait_limit(are_guide *guide, int32_t polls);
 
 typedef struct are_guide_params {

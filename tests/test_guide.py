@@ -180,3 +180,30 @@ def test_bounded_wait_gives_up_and_the_next_call_succeeds(gpu_lib, oracle):
     out = g.forward(feat)
     ref = oracle.guide_forward(g.params, feat)
     assert np.abs(out[:, :40] - ref[:, :40]).max() < 0.05 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.gpu
+def test_training_wait_gives_up_and_the_step_is_skipped(gpu_lib, oracle):
+    """The training kernel's tensor-core waits are bounded the same way: with
+    no polls allowed for the first MMA wait, are_guide_train reports
+    ARE_ERR_KERNEL_TIMEOUT and the weights are unchanged (the step's gradients
+    are flagged and Adam skips it); with the default bound the next step
+    trains."""
+    g = are.Guide(seed=13)
+    s = random_samples(3000, 41)
+    p0 = g.params
+    g.set_wait_limit(0)
+    with pytest.raises(are.AreError) as e:
+        g.train(s, lr=1e-2)
+    assert e.value.status == 5 and "16" in str(e.value)
+    with pytest.raises(are.AreError) as e:  # the gradient alone as well
+        g.gradient(s)
+    assert e.value.status == 5
+    assert np.array_equal(g.params, p0)
+    g.set_wait_limit(-1)
+    loss = g.train(s, lr=1e-2)
+    assert np.isfinite(loss)
+    assert not np.array_equal(g.params, p0)
+    _, grad = g.gradient(s)
+    _, rgrad = oracle.guide_loss_grad(g.params, s)
+    assert np.dot(grad, rgrad) / (np.linalg.norm(grad) * np.linalg.norm(rgrad)) > 0.995
