@@ -137,6 +137,23 @@ def test_megakernel_mesh_equals_wavefront(gpu_lib):
     assert sa["segments"] == sb["segments"] and sa["error_word"] == sb["error_word"] == 0
 
 
+def test_mesh_tail_with_more_paths_than_threads(gpu_lib):
+    """A wavefront render whose tail launch can get more queued paths than
+    the 4-wide megakernel has resident threads (a 2M-path pool over 4M work
+    items: the tail takes over once every item is taken and at most a
+    quarter of the pool is queued), so threads may run several queue entries
+    one after another through the interleaved walks: the image is still the
+    megakernel schedule's bit for bit."""
+    s, cam, par = small(are.CONFIG_MESH, 1024, 1024, 4, chunk=1)
+    sc = are.Scene(s)
+    a, va, sa = sc.render(cam, dict(par, schedule=are.SCHEDULE_WAVEFRONT, pool_size=1 << 21))
+    b, vb, sb = sc.render(cam, dict(par, schedule=are.SCHEDULE_MEGAKERNEL))
+    assert sa["aux"][0] > 0  # the tail launch traced the last paths
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    assert sa["segments"] == sb["segments"] and sa["error_word"] == sb["error_word"] == 0
+
+
 def test_schedule_argument(gpu_lib):
     s, cam, par = small(are.CONFIG_CORNELL, 16, 16, 4)
     sc = are.Scene(s)
