@@ -81,6 +81,7 @@ struct DevScene {
 	int32_t background, triangle_test;
 	float bg_a[3], bg_b[3];
 	float box_pad;             // absolute padding applied to every node box
+	int32_t interleave;        // megakernels interleave the lanes' binary-tree walks (scenes with quads or triangles)
 };
 
 }  // namespace are_core

@@ -259,7 +259,7 @@ __device__ __forceinline__ bool guided_step(const DevScene &S, const Wave &W, co
 // instantiation that records training samples (a render with a frozen network runs the one without,
 // a smaller loop).
 template <bool LINEAR, bool WIDE, bool TRAIN>
-__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
+__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE, WIDE))
 	k_guided_tail(DevScene S, Wave W, GuidedMega G) {
 	__shared__ float4 snodes[LINEAR ? 6 * LINEAR_MAX : WIDE ? 8 * TAIL_SMEM_NODES4 : 2 * SMEM_NODES];
 	__shared__ WarpHitScratch scratch[LINEAR ? BLOCK / 32 : 1];
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
 		PathState P{};
 		GuideTrack T{ 1.0f, 0u, false };
 		float4 sm{}, cm{}, q{};
-		interleaved_walks<SHORT>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
+		interleaved_walks<SHORT, true>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
 			n, gridDim.x * blockDim.x, P, err, segments,
 			[&](unsigned i) {
 				P = load_path(W, 0, i);

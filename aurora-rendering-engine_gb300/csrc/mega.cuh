@@ -25,17 +25,17 @@ constexpr int WALK_READY_LANES = 20;
 //   begin_entry(i): loads queue entry i into P (and whatever the caller keeps per entry)
 //   shade(h):       one bounce of P at hit h = (t, leaf bits, u, v); true if P holds a ray to trace
 //   end_entry():    the entry's slot has no sample left (write its sums back)
-template <int SHORT, class Begin, class Shade, class End>
+template <int SHORT, bool WIDE, class Begin, class Shade, class End>
 __device__ __forceinline__ void interleaved_walks(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes,
 	int4 *__restrict__ sstack, float tmin, unsigned i, unsigned n, unsigned stride, const PathState &P, uint32_t &err,
 	unsigned long long &segments, Begin begin_entry, Shade shade, End end_entry) {
 	const float inf = __int_as_float(0x7f800000);
-	WalkStack<MAX_STACK4 - SHORT> st;
+	WalkStack<(WIDE ? MAX_STACK4 : MAX_STACK) - SHORT> st;
 	Walk w;
 	bool live = i < n, walking = false;
 	if (live) {
 		begin_entry(i);
-		walking = walk4_begin(S, P.o, P.d, tmin, inf, w);
+		walking = WIDE ? walk4_begin(S, P.o, P.d, tmin, inf, w) : walk2_begin(S, snodes, n_snodes, P.o, P.d, tmin, inf, w);
 	}
 	while (__any_sync(0xffffffffu, live)) {
 		for (;;) {
@@ -44,8 +44,12 @@ __device__ __forceinline__ void interleaved_walks(const DevScene &S, const float
 			if (walkers == 0 || __popc(ready) >= WALK_READY_LANES) break;
 			const unsigned at_leaf = __ballot_sync(0xffffffffu, walking && w.b > 0);
 			const bool leaf_round = 2 * __popc(at_leaf) >= __popc(walkers);
-			if (walking && (w.b > 0) == leaf_round)
-				walking = walk4_step<SHORT>(S, snodes, n_snodes, P.o, P.d, tmin, inf, err, sstack, st, w);
+			if (walking && (w.b > 0) == leaf_round) {
+				if constexpr (WIDE)
+					walking = walk4_step<SHORT>(S, snodes, n_snodes, P.o, P.d, tmin, inf, err, sstack, st, w);
+				else
+					walking = walk2_step<SHORT>(S, snodes, n_snodes, P.o, P.d, tmin, inf, err, sstack, st, w);
+			}
 		}
 		if (live && !walking) {
 			++segments;
@@ -58,7 +62,8 @@ __device__ __forceinline__ void interleaved_walks(const DevScene &S, const float
 					live = true;
 				}
 			}
-			if (live) walking = walk4_begin(S, P.o, P.d, tmin, inf, w);
+			if (live)
+				walking = WIDE ? walk4_begin(S, P.o, P.d, tmin, inf, w) : walk2_begin(S, snodes, n_snodes, P.o, P.d, tmin, inf, w);
 		}
 	}
 }

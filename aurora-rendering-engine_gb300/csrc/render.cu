@@ -225,10 +225,13 @@ __global__ void __launch_bounds__(BLOCK) k_shade(DevScene S, Wave W, int par) {
 // holds one camera path per resident thread).
 //
 // One instantiation per closest-hit strategy (LINEAR: the staged linear scan of
-// a scene with at most LINEAR_MAX primitives, else the BVH), each with the
-// occupancy that measured fastest for it.
-template <bool LINEAR, bool WIDE = false>
-__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
+// a scene with at most LINEAR_MAX primitives, else the BVH: WIDE the 4-wide
+// tree, INTER the lanes' walks interleaved (mega.cuh) rather than one walk per
+// ray and bounce; the 4-wide tree always interleaves, a binary tree does for
+// scenes with quads or triangles, measured faster there and slower on sphere
+// fields), each with the occupancy that measured fastest for it.
+template <bool LINEAR, bool WIDE = false, bool INTER = WIDE>
+__global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE, INTER))
 	k_tail(DevScene S, Wave W, int par) {
 	// linear scenes: the staged primitives and leaf boxes (6 float4 per primitive at most) and
 	// one closest-hit scratch per warp; BVH scenes: the top BVH levels
@@ -276,10 +279,10 @@ __global__ void __launch_bounds__(BLOCK, tail_min_blocks(LINEAR, WIDE))
 			}
 			if (i < n) W.acc_s[slot] = sm, W.acc_c[slot] = cm, W.acc_q[slot] = q;
 		}
-	} else if constexpr (WIDE) {
+	} else if constexpr (WIDE || INTER) {
 		PathState P{};
 		float4 sm{}, cm{}, q{};
-		interleaved_walks<SHORT>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
+		interleaved_walks<SHORT, WIDE>(S, snodes, n_snodes, sstack + threadIdx.x, W.t_min, blockIdx.x * blockDim.x + threadIdx.x,
 			n, gridDim.x * blockDim.x, P, err, segments,
 			[&](unsigned i) {
 				P = load_path(W, par, i);
@@ -421,10 +424,12 @@ void camera_frame(const are_camera &c, int w, int h, int flags, CameraFrame &f) 
 	f.height = h;
 }
 
-// the megakernel instantiation for scene S: linear scan, 4-wide tree or binary tree
+// the megakernel instantiation for scene S: linear scan, 4-wide tree, or binary tree with interleaved
+// or per-ray walks
 static const void *tail_fn(bool linear, const DevScene &S) {
 	if (linear) return (const void *)k_tail<true>;
-	return S.n_nodes4 > 0 ? (const void *)k_tail<false, true> : (const void *)k_tail<false, false>;
+	if (S.n_nodes4 > 0) return (const void *)k_tail<false, true>;
+	return S.interleave ? (const void *)k_tail<false, false, true> : (const void *)k_tail<false, false, false>;
 }
 
 void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const Wave &W) {
@@ -432,8 +437,10 @@ void launch_tail(bool linear, int grid, cudaStream_t s, const DevScene &S, const
 		k_tail<true><<<grid, BLOCK, 0, s>>>(S, W, 0);
 	else if (S.n_nodes4 > 0)
 		k_tail<false, true><<<grid, BLOCK, 0, s>>>(S, W, 0);
+	else if (S.interleave)
+		k_tail<false, false, true><<<grid, BLOCK, 0, s>>>(S, W, 0);
 	else
-		k_tail<false, false><<<grid, BLOCK, 0, s>>>(S, W, 0);
+		k_tail<false, false, false><<<grid, BLOCK, 0, s>>>(S, W, 0);
 }
 
 int tail_grid(bool linear, const DevScene &S, int n_sms) { return grid_for(tail_fn(linear, S), n_sms); }

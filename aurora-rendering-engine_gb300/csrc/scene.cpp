@@ -407,6 +407,7 @@ are_status scene_create_device(const are_scene_desc *d, are_scene **out) {
 	S.n_textures = d->n_textures;
 	S.background = d->background;
 	S.triangle_test = d->triangle_test;
+	S.interleave = (d->n_quads + d->n_triangles) > 0 ? 1 : 0;
 	for (int k = 0; k < 3; ++k) S.bg_a[k] = d->bg_a[k], S.bg_b[k] = d->bg_b[k];
 	S.box_pad = r.box_pad;
 	sc->n_prims = n;
@@ -587,6 +588,7 @@ are_status scene_create(const are_scene_desc *d, are_scene **out) {
 	S.n_textures = d->n_textures;
 	S.background = d->background;
 	S.triangle_test = d->triangle_test;
+	S.interleave = (d->n_quads + d->n_triangles) > 0 ? 1 : 0;
 	for (int k = 0; k < 3; ++k) S.bg_a[k] = d->bg_a[k], S.bg_b[k] = d->bg_b[k];
 	S.box_pad = bvh.box_pad;
 	sc->n_prims = n;

@@ -883,6 +883,79 @@ __device__ __forceinline__ void walk_push(int4 *__restrict__ sstack, WalkStack<N
 	}
 }
 
+// Binary tree (closest_hit's walk): sets up ray (o, d); false when the walk is
+// over before it begins (no primitives, or the root's box missed).
+__device__ __forceinline__ bool walk2_begin(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
+	f3 d, float tmin, float tmax, Walk &w) {
+	walk_setup(o, d, w);
+	if (S.n_prims == 0) return false;
+	const float4 r1 = n_snodes > 0 ? snodes[1] : ldg4(S.nodes + 1);
+	const float4 r0 = n_snodes > 0 ? snodes[0] : ldg4(S.nodes + 0);
+	w.a = __float_as_int(r0.w), w.b = __float_as_int(r1.w);
+	return walk_root(w, r0, r1, tmin, tmax);
+}
+
+// Binary tree: visits the current entry and moves to the next; false when the walk is over.
+template <int SHORT>
+__device__ __forceinline__ bool walk2_step(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes, f3 o,
+	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack, WalkStack<MAX_STACK - SHORT> &st, Walk &w) {
+	if (w.steps++ > S.n_nodes) {  // a well-formed tree is walked visiting each node pair at most once
+		err |= ERR_BVH_WALK;
+		return false;
+	}
+	if (w.b == 0) {
+		// interior: both children (one 64-byte line)
+		const int c = w.a;
+		float4 c00, c01, c10, c11;
+		if (c + 1 < n_snodes) {
+			c00 = snodes[2 * c], c01 = snodes[2 * c + 1], c10 = snodes[2 * c + 2], c11 = snodes[2 * c + 3];
+		} else {
+			c00 = ldg4(S.nodes + 2 * c), c01 = ldg4(S.nodes + 2 * c + 1);
+			c10 = ldg4(S.nodes + 2 * c + 2), c11 = ldg4(S.nodes + 2 * c + 3);
+		}
+		const float bt = fminf(w.best.t * 1.0000039f, tmax * 1.0000039f);
+		float l0, l1;
+		bool h0, h1;
+		{
+			const float t0x = fmaf(c00.x, w.ix, w.ox), t1x = fmaf(c01.x, w.ix, w.ox);
+			const float t0y = fmaf(c00.y, w.iy, w.oy), t1y = fmaf(c01.y, w.iy, w.oy);
+			const float t0z = fmaf(c00.z, w.iz, w.oz), t1z = fmaf(c01.z, w.iz, w.oz);
+			l0 = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+			const float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+			h0 = l0 <= hi;
+		}
+		{
+			const float t0x = fmaf(c10.x, w.ix, w.ox), t1x = fmaf(c11.x, w.ix, w.ox);
+			const float t0y = fmaf(c10.y, w.iy, w.oy), t1y = fmaf(c11.y, w.iy, w.oy);
+			const float t0z = fmaf(c10.z, w.iz, w.oz), t1z = fmaf(c11.z, w.iz, w.oz);
+			l1 = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+			const float hi = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), bt));
+			h1 = l1 <= hi;
+		}
+		if (h0 && h1) {
+			int2 nearn = make_int2(__float_as_int(c00.w), __float_as_int(c01.w));
+			int2 farn = make_int2(__float_as_int(c10.w), __float_as_int(c11.w));
+			if (l1 < l0) {
+				const int2 t = nearn;
+				nearn = farn;
+				farn = t;
+			}
+			walk_push<SHORT>(sstack, st, w, farn, fmaxf(l0, l1), err);
+			w.a = nearn.x;
+			w.b = nearn.y;
+			return true;
+		}
+		if (h0 || h1) {
+			w.a = __float_as_int(h0 ? c00.w : c10.w);
+			w.b = __float_as_int(h0 ? c01.w : c11.w);
+			return true;
+		}
+	} else {
+		leaf_hits(S, w.a, w.b, o, d, tmin, tmax, w.best);
+	}
+	return walk_pop<SHORT>(sstack, st, w);
+}
+
 // 4-wide tree (closest_hit4's walk): sets up ray (o, d); false when the ray
 // misses the root's box (the walk is over: w.best is the miss).
 __device__ __forceinline__ bool walk4_begin(const DevScene &S, f3 o, f3 d, float tmin, float tmax, Walk &w) {

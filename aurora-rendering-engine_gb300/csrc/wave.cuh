@@ -13,14 +13,20 @@ namespace are_core {
 constexpr int GRAPH_ITERS = 8;  // iterations per graph launch (even)
 constexpr int BLOCK = 256;
 // resident blocks per SM requested for the tail / megakernel (registers per thread follow):
-// linear-scan scenes run best at 4 (64 registers); binary trees at 2 (104 registers, no spill);
-// 4-wide trees, whose walks interleave (mega.cuh), at 4 (64 registers: more warps to cover the
-// node loads of incoherent rays outweigh the spills)
+// linear-scan scenes run best at 4 (64 registers); binary trees walked ray by ray at 2 (104
+// registers, no spill); binary trees whose walks interleave (mega.cuh) at 3 (80 registers; four
+// blocks' shared memory does not fit beside their 256 staged nodes); 4-wide trees, whose walks
+// always interleave, at 4 (64 registers: more warps to cover the node loads of incoherent rays
+// outweigh the spills)
 constexpr int TAIL_MIN_BLOCKS_LINEAR = 4;
 constexpr int TAIL_MIN_BLOCKS_BVH = 2;
+constexpr int TAIL_MIN_BLOCKS_BVH_INTERLEAVED = 3;
 constexpr int TAIL_MIN_BLOCKS_WIDE = 4;
-__host__ __device__ constexpr int tail_min_blocks(bool linear, bool wide) {
-	return linear ? TAIL_MIN_BLOCKS_LINEAR : wide ? TAIL_MIN_BLOCKS_WIDE : TAIL_MIN_BLOCKS_BVH;
+__host__ __device__ constexpr int tail_min_blocks(bool linear, bool wide, bool interleaved) {
+	return linear ? TAIL_MIN_BLOCKS_LINEAR
+		 : wide   ? TAIL_MIN_BLOCKS_WIDE
+		 : interleaved ? TAIL_MIN_BLOCKS_BVH_INTERLEAVED
+					   : TAIL_MIN_BLOCKS_BVH;
 }
 // wide nodes the megakernel stages in shared memory (16 KB: four blocks per SM fit with their stacks)
 constexpr int TAIL_SMEM_NODES4 = 128;
