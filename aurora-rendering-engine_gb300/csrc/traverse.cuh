@@ -968,13 +968,20 @@ __device__ __forceinline__ bool walk4_begin(const DevScene &S, f3 o, f3 d, float
 template <int SHORT>
 __device__ __forceinline__ bool walk4_step(const DevScene &S, const float4 *__restrict__ snodes, int n_snodes4, f3 o,
 	f3 d, float tmin, float tmax, uint32_t &err, int4 *__restrict__ sstack, WalkStack<MAX_STACK4 - SHORT> &st, Walk &w) {
-	if (w.steps++ > 4 * S.n_nodes4 + 1) {  // a well-formed tree yields each entry once
+	// a well-formed tree yields each entry once, and a leaf's primitives are visited one per step
+	if (w.steps++ > 4 * S.n_nodes4 + 1 + S.n_prims) {
 		err |= ERR_BVH_WALK;
 		return false;
 	}
 	const float inf = __int_as_float(0x7f800000);
 	if (w.b > 0) {
-		leaf_hits(S, w.a, w.b, o, d, tmin, tmax, w.best);
+		// one primitive per step, so a leaf round tests one primitive in every lane taking part
+		leaf_hits(S, w.a, 1, o, d, tmin, tmax, w.best);
+		if (w.b > 1) {
+			++w.a;
+			--w.b;
+			return true;
+		}
 	} else {
 		if ((unsigned)w.a >= (unsigned)S.n_nodes4) {
 			err |= ERR_BVH_WALK;
