@@ -798,14 +798,16 @@ __device__ __forceinline__ Hit closest_hit4(const DevScene &S, const float4 *__r
 }
 
 // ---------------------------------------------------------------------------
-// The walk of closest_hit4 as a resumable state machine: walk4_begin sets a
-// ray up, each walk4_step visits one entry (a wide node or a leaf) and picks
-// the next, in the same order and with the same arithmetic, so the hit is the
-// same bit for bit.  A persistent kernel can then hold a lane whose walk has
-// ended (its hit waiting to be shaded) while the other lanes of its warp take
-// further steps, and can let only the lanes at a wide node (or only those at a
-// leaf) step at a time, instead of every lane waiting for the longest walk of
-// the warp at every bounce and every step running both kinds of visit.
+// The walks of closest_hit and closest_hit4 as resumable state machines:
+// walk2_begin / walk4_begin set a ray up, each walk2_step / walk4_step visits
+// one entry (an interior node, a leaf, or for the 4-wide tree one primitive of
+// a leaf) and picks the next, in the same order and with the same arithmetic,
+// so the hit is the same bit for bit.  A persistent kernel can then hold a lane
+// whose walk has ended (its hit waiting to be shaded, or the lane taking its
+// next ray) while the other lanes of its warp take further steps, and can let
+// only the lanes at an interior node (or only those at a leaf) step at a time,
+// instead of every lane waiting for the longest walk of the warp and every
+// step running both kinds of visit.
 
 struct Walk {
 	float ix, iy, iz, ox, oy, oz;  // reciprocal direction and -origin / direction
