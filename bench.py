@@ -291,16 +291,24 @@ def guiding_eval(budget_s: float = 0.1, params: dict | None = None) -> dict | No
                           "prior_training_s": round(t_train, 3), "adam_steps_total": len(g.loss_history()),
                           "relmse_plain_over_guided": round(ep / ew, 3)}
     # cold start: a fresh network, training inside the budget, on GUIDE_COLD_BATCH-sample batches and on
-    # the warm start's
+    # the warm start's.  What a fresh network learns in 0.1 s varies from network to network, so three
+    # (seeds 1, 2, 3) render at the fitted spp and the median is reported beside each run
     for key, batch in (("guided_cold", GUIDE_COLD_BATCH), ("guided_cold_same_batch", settings["batch"])):
         gpc = are.GuideParams.make(**dict(settings, batch=batch))
         (gc, _, cst), t_c, spp_c = fit(lambda n: sc.render_guided(are.Guide(seed=1), cam, dict(par, spp=n, seed=1), gpc,
                                                                   with_var=False))
-        ec = relmse(gc)
-        out[key] = {"batch": batch, "spp": spp_c, "seconds": round(t_c, 3), "relmse": round(ec, 7),
-                    "adam_steps": cst["train_steps"], "passes": cst["iterations"],
-                    "kernel_ms": {k: round(v, 2) for k, v in cst["kernel_ms"].items()},
-                    "relmse_plain_over_guided": round(ep / ec, 3)}
+        runs = [(1, relmse(gc), t_c, cst)]
+        for k in (2, 3):
+            (gk, _, sk), tk = timed(lambda: sc.render_guided(are.Guide(seed=k), cam, dict(par, spp=spp_c, seed=k), gpc,
+                                                             with_var=False))
+            runs.append((k, relmse(gk), tk, sk))
+        mid = sorted(runs, key=lambda r: r[1])[1]
+        out[key] = {"batch": batch, "spp": spp_c, "seconds": round(mid[2], 3), "relmse": round(mid[1], 7),
+                    "adam_steps": mid[3]["train_steps"], "passes": mid[3]["iterations"],
+                    "kernel_ms": {k: round(v, 2) for k, v in mid[3]["kernel_ms"].items()},
+                    "relmse_plain_over_guided": round(ep / mid[1], 3), "of": "median of three fresh networks",
+                    "runs": [{"guide_seed": r[0], "seconds": round(r[2], 3), "relmse_plain_over_guided": round(ep / r[1], 3)}
+                             for r in runs]}
     out["relmse_plain_over_guided"] = out["guided_warm"]["relmse_plain_over_guided"]
     out["headline_start"] = "warm"
     sc.close()
